@@ -1,0 +1,162 @@
+"""Host-side scene container: the flattened arrays GLSLPT::Scene hands to its
+Renderer (src/core/Scene.h:87-125), as numpy arrays.
+
+`SceneData.desc()` builds the `pt_scene_desc` of include/pt_cuda.h pointing
+at those arrays (the arrays must outlive any call that uses the descriptor).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+F = np.float32
+I = np.int32
+
+
+@dataclass
+class SceneData:
+    bvh_nodes: np.ndarray          # (N, 9) float32: bboxmin, bboxmax, LRLeaf
+    top_level_index: int
+    vert_indices: np.ndarray       # (T, 3) int32
+    vertices_uvx: np.ndarray       # (V, 4) float32
+    normals_uvy: np.ndarray        # (V, 4) float32
+    transforms: np.ndarray         # (I, 16) float32 (Mat4 rows)
+    materials: np.ndarray          # (M, 32) float32
+    lights: np.ndarray             # (L, 15) float32
+    envmap_rgb: np.ndarray | None = None   # (H, W, 3) float32
+    envmap_cdf: np.ndarray | None = None   # (H, W) float32
+    envmap_total_sum: float = 0.0
+    texture_maps: np.ndarray | None = None  # (K, h, w, 4) uint8
+    options: dict = field(default_factory=dict)
+    camera: dict = field(default_factory=dict)
+    # instance description kept for TLAS rebuilds: mesh id / material id per instance
+    instance_mesh: np.ndarray | None = None
+    instance_material: np.ndarray | None = None
+
+    def __post_init__(self):
+        self.bvh_nodes = np.ascontiguousarray(self.bvh_nodes, F).reshape(-1, 9)
+        self.vert_indices = np.ascontiguousarray(self.vert_indices, I).reshape(-1, 3)
+        self.vertices_uvx = np.ascontiguousarray(self.vertices_uvx, F).reshape(-1, 4)
+        self.normals_uvy = np.ascontiguousarray(self.normals_uvy, F).reshape(-1, 4)
+        self.transforms = np.ascontiguousarray(self.transforms, F).reshape(-1, 16)
+        self.materials = np.ascontiguousarray(self.materials, F).reshape(-1, 32)
+        self.lights = np.ascontiguousarray(self.lights, F).reshape(-1, 15)
+        if self.envmap_rgb is not None:
+            self.envmap_rgb = np.ascontiguousarray(self.envmap_rgb, F)
+            self.envmap_cdf = np.ascontiguousarray(self.envmap_cdf, F)
+
+    # ------------------------------------------------------------------
+    @property
+    def num_tris(self) -> int:
+        return int(self.vert_indices.shape[0])
+
+    def desc(self) -> capi.pt_scene_desc:
+        d = capi.pt_scene_desc()
+
+        def fp(a):
+            return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None and a.size else None
+
+        d.bvh_nodes = fp(self.bvh_nodes)
+        d.num_bvh_nodes = self.bvh_nodes.shape[0]
+        d.top_level_index = int(self.top_level_index)
+        d.vert_indices = self.vert_indices.ctypes.data_as(C.POINTER(C.c_int32)) if self.vert_indices.size else None
+        d.num_tris = self.vert_indices.shape[0]
+        d.vertices_uvx = fp(self.vertices_uvx)
+        d.normals_uvy = fp(self.normals_uvy)
+        d.num_vertices = self.vertices_uvx.shape[0]
+        d.transforms = fp(self.transforms)
+        d.num_instances = self.transforms.shape[0]
+        d.materials = fp(self.materials)
+        d.num_materials = self.materials.shape[0]
+        d.lights = fp(self.lights)
+        d.num_lights = self.lights.shape[0]
+        if self.envmap_rgb is not None:
+            d.envmap_rgb = fp(self.envmap_rgb)
+            d.envmap_cdf = fp(self.envmap_cdf)
+            d.envmap_height, d.envmap_width = self.envmap_rgb.shape[:2]
+            d.envmap_total_sum = float(self.envmap_total_sum)
+        if self.texture_maps is not None and self.texture_maps.size:
+            self.texture_maps = np.ascontiguousarray(self.texture_maps, np.uint8)
+            d.texture_maps = self.texture_maps.ctypes.data_as(C.POINTER(C.c_uint8))
+            d.num_textures, d.tex_height, d.tex_width = self.texture_maps.shape[:3]
+        self._desc_keepalive = d
+        return d
+
+    def render_options(self, **overrides) -> capi.pt_render_options:
+        o = dict(self.options)
+        o.update(overrides)
+        return capi.make_options(**o)
+
+    def pt_camera(self) -> capi.pt_camera:
+        c = self.camera
+        return capi.make_camera(c["position"], c["up"], c["right"], c["forward"], c["fov"],
+                                c.get("focal_dist", 0.1), c.get("aperture", 0.0))
+
+    # ------------------------------------------------------------------
+    def save_npz(self, path: str):
+        arrays = dict(bvh_nodes=self.bvh_nodes, vert_indices=self.vert_indices, vertices_uvx=self.vertices_uvx,
+                      normals_uvy=self.normals_uvy, transforms=self.transforms, materials=self.materials,
+                      lights=self.lights)
+        if self.envmap_rgb is not None:
+            arrays["envmap_rgb"] = self.envmap_rgb
+            arrays["envmap_cdf"] = self.envmap_cdf
+        meta = dict(top_level_index=int(self.top_level_index), envmap_total_sum=float(self.envmap_total_sum),
+                    options=self.options, camera=self.camera)
+        np.savez_compressed(path, meta=np.frombuffer(json.dumps(meta).encode(), np.uint8), **arrays)
+
+    @staticmethod
+    def load_npz(path: str) -> "SceneData":
+        z = np.load(path)
+        meta = json.loads(bytes(z["meta"]).decode())
+        return SceneData(
+            bvh_nodes=z["bvh_nodes"], top_level_index=meta["top_level_index"], vert_indices=z["vert_indices"],
+            vertices_uvx=z["vertices_uvx"], normals_uvy=z["normals_uvy"], transforms=z["transforms"],
+            materials=z["materials"], lights=z["lights"],
+            envmap_rgb=z["envmap_rgb"] if "envmap_rgb" in z else None,
+            envmap_cdf=z["envmap_cdf"] if "envmap_cdf" in z else None,
+            envmap_total_sum=meta["envmap_total_sum"], options=meta["options"], camera=meta["camera"])
+
+
+def load_ref_dump(prefix: str) -> SceneData:
+    """Read the <prefix>.json / <prefix>.bin pair written by the reference
+    scene dumper (oracle/ref_host/ref_scene_dump.cpp)."""
+    with open(prefix + ".json") as fh:
+        m = json.load(fh)
+    assert m["sizeof_node"] == 36 and m["sizeof_material"] == 128 and m["sizeof_light"] == 60
+    raw = open(prefix + ".bin", "rb").read()
+    off = 0
+
+    def take(dtype, count):
+        nonlocal off
+        nbytes = np.dtype(dtype).itemsize * count
+        a = np.frombuffer(raw, dtype, count, off).copy()
+        off += nbytes
+        return a
+
+    nodes = take(F, 9 * m["num_bvh_nodes"])
+    idx = take(I, 3 * m["num_tris"])
+    verts = take(F, 4 * m["num_vertices"])
+    norms = take(F, 4 * m["num_vertices"])
+    xf = take(F, 16 * m["num_instances"])
+    mats = take(F, 32 * m["num_materials"])
+    lights = take(F, 15 * m["num_lights"])
+    env = cdf = None
+    if m["envmap_width"]:
+        w, h = m["envmap_width"], m["envmap_height"]
+        env = take(F, 3 * w * h).reshape(h, w, 3)
+        cdf = take(F, w * h).reshape(h, w)
+    tex = None
+    if m["num_textures"]:
+        tex = take(np.uint8, 4 * m["tex_width"] * m["tex_height"] * m["num_textures"]).reshape(
+            m["num_textures"], m["tex_height"], m["tex_width"], 4)
+    assert off == len(raw), (off, len(raw))
+    return SceneData(bvh_nodes=nodes, top_level_index=m["top_level_index"], vert_indices=idx, vertices_uvx=verts,
+                     normals_uvy=norms, transforms=xf, materials=mats, lights=lights, envmap_rgb=env, envmap_cdf=cdf,
+                     envmap_total_sum=m["envmap_total_sum"], texture_maps=tex, options=m["options"],
+                     camera=m["camera"])

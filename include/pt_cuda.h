@@ -1,0 +1,231 @@
+/*
+ * pt_cuda.h - C ABI of the GB300 path-tracing library (libptgb.so).
+ *
+ * The library replaces the device half of GLSL-PathTracer's renderer: the
+ * class GLSLPT::Renderer (src/core/Renderer.h:104-185) that uploads the
+ * flattened scene into GL buffers/textures and runs tile.glsl per pixel.
+ * Every entry point below takes plain pointers and sizes; buffers passed in
+ * are HOST memory unless the name says otherwise.  All calls return 0
+ * (PT_OK) on success or a PT_ERR_* code; pt_last_error() gives the message.
+ *
+ * Data layouts are exactly the reference's host arrays, so a caller hands over
+ * what GLSLPT::Scene::ProcessScene (src/core/Scene.cpp:216-297) produced:
+ *   bvh_nodes     RadeonRays::BvhTranslator::Node, 9 floats each
+ *                 (thirdparty/RadeonRays/bvh_translator.h:45-50):
+ *                 bboxmin.xyz, bboxmax.xyz, LRLeaf.xyz (ints stored as floats)
+ *   vert_indices  GLSLPT::Indices {x,y,z} per triangle (src/core/Scene.h:61-64)
+ *   vertices_uvx  Vec4 position + u per vertex (src/core/Scene.h:94)
+ *   normals_uvy   Vec4 normal + v per vertex (src/core/Scene.h:95)
+ *   transforms    Mat4 per instance, row-vector layout, translation in
+ *                 data[3][0..2] (src/math/Mat4.h:30-62)
+ *   materials     GLSLPT::Material, 32 floats (src/core/Material.h:47-119)
+ *   lights        GLSLPT::Light, 15 floats (src/core/Scene.h:50-59)
+ *   envmap        EnvironmentMap img (RGB float) + cdf (src/core/EnvironmentMap.h)
+ *
+ * Images are W*H float4 / uchar4 with row 0 at the BOTTOM (GL convention,
+ * as glGetTexImage returns them in Renderer::GetOutputBuffer,
+ * src/core/Renderer.cpp:619-634).
+ *
+ * Threading: one context = one CUDA stream; calls on one context must be
+ * serialised by the caller (the reference renderer is single-threaded).
+ */
+#ifndef PT_CUDA_H
+#define PT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PT_OK                 0
+#define PT_ERR_INVALID_ARG    1  /* null pointer, bad size, bad index in scene data */
+#define PT_ERR_CUDA           2  /* a CUDA runtime call failed */
+#define PT_ERR_OUT_OF_MEMORY  3  /* device allocation failed */
+#define PT_ERR_STACK_OVERFLOW 4  /* traversal stack limit hit (kernel status word) */
+#define PT_ERR_UNSUPPORTED    5  /* scene feature the kernels do not implement */
+#define PT_ERR_TIMEOUT        6  /* a bounded device wait ran out */
+#define PT_ERR_QUEUE_OVERFLOW 7  /* wavefront queue capacity exceeded */
+
+/* ---- scene description: the reference's flattened host arrays ---------- */
+typedef struct pt_scene_desc {
+    const float*   bvh_nodes;        /* 9 floats per node */
+    int32_t        num_bvh_nodes;
+    int32_t        top_level_index;  /* BvhTranslator::topLevelIndex */
+    const int32_t* vert_indices;     /* 3 int32 per triangle */
+    int32_t        num_tris;
+    const float*   vertices_uvx;     /* 4 floats per vertex */
+    const float*   normals_uvy;      /* 4 floats per vertex */
+    int32_t        num_vertices;
+    const float*   transforms;       /* 16 floats per instance */
+    int32_t        num_instances;
+    const float*   materials;        /* 32 floats per material */
+    int32_t        num_materials;
+    const float*   lights;           /* 15 floats per light */
+    int32_t        num_lights;
+    const float*   envmap_rgb;       /* envmap_width*envmap_height*3 floats, or NULL */
+    const float*   envmap_cdf;       /* envmap_width*envmap_height floats */
+    int32_t        envmap_width;
+    int32_t        envmap_height;
+    float          envmap_total_sum;
+    const uint8_t* texture_maps;     /* num_textures * tex_width*tex_height*4 bytes, or NULL */
+    int32_t        tex_width;
+    int32_t        tex_height;
+    int32_t        num_textures;
+} pt_scene_desc;
+
+/* Mirror of GLSLPT::RenderOptions (src/core/Renderer.h:37-100); booleans are
+ * 0/1 ints.  Fields that only drive the window/UI are left out. */
+typedef struct pt_render_options {
+    int32_t render_width, render_height;
+    int32_t tile_width, tile_height;
+    int32_t max_depth;
+    int32_t max_spp;                 /* -1: unlimited */
+    int32_t rr_depth;
+    int32_t enable_rr;
+    int32_t enable_envmap;
+    int32_t enable_uniform_light;
+    int32_t hide_emitters;
+    int32_t enable_background;
+    int32_t transparent_background;
+    int32_t enable_roughness_mollification;
+    int32_t enable_volume_mis;
+    int32_t opengl_normal_map;
+    int32_t enable_tonemap;
+    int32_t enable_aces;
+    int32_t simple_aces_fit;
+    float   uniform_light_col[3];
+    float   background_col[3];
+    float   envmap_intensity;
+    float   envmap_rot;              /* degrees, as in RenderOptions::envMapRot */
+    float   roughness_mollification_amt;
+} pt_render_options;
+
+/* GLSLPT::Camera fields read by the shaders (src/core/Camera.h:41-50);
+ * fov in radians, as Camera stores it. */
+typedef struct pt_camera {
+    float position[3];
+    float up[3];
+    float right[3];
+    float forward[3];
+    float fov;
+    float focal_dist;
+    float aperture;
+} pt_camera;
+
+/* One ray of a ray set (test hook for ClosestHit / AnyHit). */
+typedef struct pt_ray {
+    float origin[3];
+    float direction[3];
+} pt_ray;
+
+/* Result of a closest-hit query over the triangle BVH.  prim_id is the
+ * index into vert_indices (the global triangle index the reference reads at
+ * closest_hit.glsl:122), inst_id the instance (-leaf-1 of the TLAS leaf),
+ * both -1 on a miss; t is the hit distance (INF = 1e6 on a miss). */
+typedef struct pt_hit {
+    float   t;
+    float   u, v;                    /* barycentrics uvt.x, uvt.y */
+    int32_t prim_id;
+    int32_t inst_id;
+} pt_hit;
+
+/* Counters of the last render call. */
+typedef struct pt_stats {
+    uint64_t closest_rays;           /* executed closest-hit queries */
+    uint64_t shadow_rays;            /* executed any-hit queries / transmittance segments */
+    uint64_t paths;                  /* camera paths traced */
+    float    kernel_ms;              /* device time of the last render call (CUDA events) */
+    int32_t  status;                 /* device status word of the last call (PT_OK or PT_ERR_*) */
+} pt_stats;
+
+#define PT_INTEGRATOR_MEGAKERNEL 0
+#define PT_INTEGRATOR_WAVEFRONT  1
+
+typedef struct pt_context pt_context;
+
+/* Replaces: Renderer::Renderer(Scene*, shadersDir) -> InitGPUDataBuffers
+ * (src/core/Renderer.cpp:41-87, 135-249).  Copies the scene to the device,
+ * repacks the BVH into the device layout and allocates the accumulation
+ * buffer for options->render_width x render_height. */
+int pt_create(const pt_scene_desc* scene, const pt_render_options* options,
+              pt_context** out_ctx);
+
+/* Replaces: Renderer::~Renderer (src/core/Renderer.cpp:89-133). */
+int pt_destroy(pt_context* ctx);
+
+/* Run the context's work on a caller-owned stream (cudaStream_t passed as a
+ * pointer); NULL restores the context's own stream. */
+int pt_set_stream(pt_context* ctx, void* cuda_stream);
+
+/* Replaces: the per-frame camera uniforms of Renderer::Update
+ * (src/core/Renderer.cpp:766-772). */
+int pt_set_camera(pt_context* ctx, const pt_camera* camera);
+
+/* Replaces: Renderer::ReloadShaders / ResizeRenderer option handling
+ * (src/core/Renderer.cpp:252-279, 380-544).  A change of resolution or tile
+ * size reallocates and clears the accumulation buffer. */
+int pt_set_options(pt_context* ctx, const pt_render_options* options);
+
+/* Chooses the kernel form used by pt_render_* (PT_INTEGRATOR_*). */
+int pt_set_integrator(pt_context* ctx, int32_t integrator);
+
+/* Replaces: the instancesModified branch of Renderer::Update
+ * (src/core/Renderer.cpp:649-665): new transforms, materials and the TLAS
+ * slice nodes[top_level_index..num_bvh_nodes) of the flattened BVH. */
+int pt_update_instances(pt_context* ctx, const float* transforms, int32_t num_instances,
+                        const float* materials, int32_t num_materials,
+                        const float* tlas_nodes, int32_t num_tlas_nodes);
+
+/* Replaces: the envMapModified branch of Renderer::Update
+ * (src/core/Renderer.cpp:668-690). */
+int pt_update_envmap(pt_context* ctx, const float* rgb, const float* cdf,
+                     int32_t width, int32_t height, float total_sum);
+
+/* Replaces: the accumTexture clear of Renderer::Update when the scene is
+ * dirty (src/core/Renderer.cpp:733-744). */
+int pt_clear_accum(pt_context* ctx);
+
+/* Replaces: one tile pass of Renderer::Render (src/core/Renderer.cpp:567-580):
+ * traces one sample for every pixel of tile (tile_x, tile_y) with the RNG
+ * frame number frame_num and adds it to the accumulation buffer. */
+int pt_render_tile(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t frame_num);
+
+/* Whole-frame form of the same work: sample passes first_pass ..
+ * first_pass+num_passes-1, each pass being every tile in the reference's
+ * order (Renderer.cpp:745-762), with the frame numbers the tile state machine
+ * would have used for them.  Equal, sample for sample, to calling
+ * pt_render_tile for each tile in turn. */
+int pt_render_passes(pt_context* ctx, int32_t first_pass, int32_t num_passes);
+
+/* Read the float4 accumulation (sum of samples, alpha in .w) into host
+ * memory: render_width*render_height*4 floats. */
+int pt_get_accum(pt_context* ctx, float* host_rgba);
+
+/* Replaces: tonemap.glsl + Renderer::GetOutputBuffer (src/shaders/tonemap.glsl:97-133,
+ * src/core/Renderer.cpp:619-634): accum / num_samples, tonemapped and gamma
+ * corrected, written as RGBA8 into host memory (w*h*4 bytes, bottom row first). */
+int pt_get_output(pt_context* ctx, int32_t num_samples, uint8_t* host_rgba8);
+
+/* Test hook: closest-hit queries (closest_hit.glsl:25-266, triangle part)
+ * over the device BVH for n host rays. */
+int pt_trace_rays(pt_context* ctx, const pt_ray* rays, int32_t n, pt_hit* hits);
+
+/* Test hook: any-hit queries (anyhit.glsl:25-216) for n host rays with
+ * per-ray max distances; occluded[i] = 1 if something is hit before max_dist[i]. */
+int pt_trace_shadow(pt_context* ctx, const pt_ray* rays, const float* max_dist,
+                    int32_t n, uint8_t* occluded);
+
+/* Counters and device time of the last pt_render_* call. */
+int pt_get_stats(pt_context* ctx, pt_stats* stats);
+
+/* Copy the last error message of this thread into buf (always terminated). */
+int pt_last_error(char* buf, size_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_CUDA_H */
