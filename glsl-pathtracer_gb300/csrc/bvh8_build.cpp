@@ -1,0 +1,553 @@
+// bvh8_build.cpp - host-side collapse of the reference's flattened binary BVH
+// into the 8-wide quantised layout of bvh8.h.
+//
+// Input is exactly what GLSLPT::Scene::ProcessScene leaves in
+// bvhTranslator.nodes (thirdparty/RadeonRays/bvh_translator.cpp:32-120):
+// pre-order binary nodes with LRLeaf = (left, right, 0) for interior nodes,
+// (firstTri, numTris, 1) for BLAS leaves and (blasRoot, materialID,
+// -instance-1) for TLAS leaves, BLASes first and the TLAS from
+// topLevelIndex on.  The wide tree keeps the binary tree's boxes: each wide
+// node takes up to eight binary descendants, chosen greedily by expanding the
+// interior child of largest surface area (so the wide tree visits the same
+// triangles the binary one does, with fewer, larger node fetches).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/pt_cuda.h"
+#include "bvh8.h"
+
+using namespace ptgb;
+
+namespace {
+
+struct BinNode {
+    float lo[3], hi[3];
+    int l, r, leaf;
+};
+
+struct Box {
+    float lo[3], hi[3];
+    void empty() { for (int k = 0; k < 3; ++k) { lo[k] = INFINITY; hi[k] = -INFINITY; } }
+    void grow(const Box& b) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], b.lo[k]); hi[k] = std::max(hi[k], b.hi[k]); }
+    }
+    void grow(const float* p) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+    }
+    double area() const {
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = std::max(0.0, double(hi[k]) - double(lo[k]));
+        return 2.0 * (d[0] * d[1] + d[1] * d[2] + d[2] * d[0]);
+    }
+};
+
+// A child candidate of a wide node: a binary interior node, or a primitive
+// range [first, first+count) (triangles in a BLAS, one instance in the TLAS).
+struct Child {
+    int bin = -1;        // binary interior node index (range children: -1)
+    int first = 0, count = 0;
+    int blas_root = -1, material = 0;  // TLAS leaf data
+    Box box;
+    bool is_range() const { return bin < 0; }
+    bool is_leaf_slot() const { return bin < 0 && count <= 3; }
+};
+
+struct Impl {
+    std::vector<BinNode> bn;
+    std::vector<WideNode> nodes;
+    std::vector<WideTri> tris;
+    std::vector<InstRef> insts;
+    std::vector<int> inst_identity;
+    std::map<int, int> blas_root_map;  // binary BLAS root -> wide node index
+    int blas_node_count = 0;
+    int blas_tri_count = 0;
+    const int32_t* vidx = nullptr;
+    const float* verts = nullptr;
+    int num_tris = 0, num_vertices = 0, num_instances = 0;
+    bool tlas = false;
+    int max_depth = 0;
+    std::string err;
+};
+
+struct BuildError {
+    std::string msg;
+};
+
+[[noreturn]] void fail(const std::string& m) { throw BuildError{m}; }
+
+Box tri_box(Impl& I, int t) {
+    if (t < 0 || t >= I.num_tris) fail("leaf triangle index out of range: " + std::to_string(t));
+    Box b;
+    b.empty();
+    for (int k = 0; k < 3; ++k) {
+        int v = I.vidx[3 * (size_t)t + k];
+        if (v < 0 || v >= I.num_vertices) fail("vertex index out of range: " + std::to_string(v));
+        b.grow(I.verts + 4 * (size_t)v);
+    }
+    return b;
+}
+
+Box range_box(Impl& I, int first, int count) {
+    Box b;
+    b.empty();
+    for (int i = 0; i < count; ++i) b.grow(tri_box(I, first + i));
+    return b;
+}
+
+Box node_box(const BinNode& n) {
+    Box b;
+    for (int k = 0; k < 3; ++k) { b.lo[k] = n.lo[k]; b.hi[k] = n.hi[k]; }
+    return b;
+}
+
+// Children contributed by binary node `b` (one entry, or leaf ranges).
+void children_of(Impl& I, int b, std::vector<Child>& out) {
+    if (b < 0 || b >= (int)I.bn.size()) fail("child node index out of range: " + std::to_string(b));
+    const BinNode& n = I.bn[b];
+    Child c;
+    if (n.leaf == 0) {
+        c.bin = b;
+        c.box = node_box(n);
+        out.push_back(c);
+    } else if (n.leaf > 0) {
+        if (I.tlas) fail("BLAS leaf reached while walking the TLAS (node " + std::to_string(b) + ")");
+        if (n.r < 0) fail("negative triangle count in leaf " + std::to_string(b));
+        if (n.r == 0) return;
+        c.first = n.l;
+        c.count = n.r;
+        // a reference leaf holds < 4 triangles and its box bounds them; bigger
+        // leaves are split into ranges later, with boxes from the triangles
+        c.box = n.r <= 3 ? node_box(n) : range_box(I, n.l, n.r);
+        if (n.r <= 3) {
+            Box tb = range_box(I, n.l, n.r);  // validates indices
+            (void)tb;
+        }
+        out.push_back(c);
+    } else {
+        if (!I.tlas) fail("TLAS leaf reached inside a BLAS (node " + std::to_string(b) + ")");
+        int inst = -n.leaf - 1;
+        if (inst >= I.num_instances) fail("instance index out of range: " + std::to_string(inst));
+        c.first = inst;
+        c.count = 1;
+        c.blas_root = n.l;
+        c.material = n.r;
+        c.box = node_box(n);
+        out.push_back(c);
+    }
+}
+
+// Split a primitive range of more than 3 primitives into up to 8 pieces.
+void split_range(Impl& I, const Child& c, std::vector<Child>& out) {
+    int pieces = std::min(8, (c.count + 2) / 3);
+    int per = (c.count + pieces - 1) / pieces;
+    for (int f = c.first; f < c.first + c.count; f += per) {
+        Child r;
+        r.first = f;
+        r.count = std::min(per, c.first + c.count - f);
+        r.box = range_box(I, r.first, r.count);
+        out.push_back(r);
+    }
+}
+
+void quantise(const Box& node, const std::vector<Child>& kids, const int slot_of[8], WideNode& wn, int imask,
+              int child_base, int prim_base, const uint8_t meta[8]) {
+    std::memset(&wn, 0, sizeof wn);
+    int ex[3];
+    double scale[3];
+    for (int k = 0; k < 3; ++k) {
+        double range = double(node.hi[k]) - double(node.lo[k]);
+        int e;
+        if (!(range > 0.0)) e = -126;
+        else {
+            e = (int)std::ceil(std::log2(range / 255.0));
+            while (std::ldexp(255.0, e) < range) ++e;
+            while (e > -126 && std::ldexp(255.0, e - 1) >= range) --e;
+        }
+        e = std::max(-126, std::min(127, e));
+        ex[k] = e;
+        scale[k] = std::ldexp(1.0, e);
+    }
+    float p[3] = {node.lo[0], node.lo[1], node.lo[2]};
+    std::memcpy(&wn.w[0], &p[0], 4);
+    std::memcpy(&wn.w[1], &p[1], 4);
+    std::memcpy(&wn.w[2], &p[2], 4);
+    wn.w[3] = uint32_t(ex[0] + 127) | (uint32_t(ex[1] + 127) << 8) | (uint32_t(ex[2] + 127) << 16) |
+              (uint32_t(imask) << 24);
+    wn.w[4] = uint32_t(child_base);
+    wn.w[5] = uint32_t(prim_base);
+    wn.w[6] = meta[0] | (meta[1] << 8) | (meta[2] << 16) | (uint32_t(meta[3]) << 24);
+    wn.w[7] = meta[4] | (meta[5] << 8) | (meta[6] << 16) | (uint32_t(meta[7]) << 24);
+    uint8_t* q = reinterpret_cast<uint8_t*>(&wn.w[8]);  // 48 bytes: qlo x,y,z then qhi x,y,z, 8 each
+    for (size_t i = 0; i < kids.size(); ++i) {
+        int s = slot_of[i];
+        for (int k = 0; k < 3; ++k) {
+            double lo = std::floor((double(kids[i].box.lo[k]) - double(p[k])) / scale[k]);
+            double hi = std::ceil((double(kids[i].box.hi[k]) - double(p[k])) / scale[k]);
+            lo = std::max(0.0, std::min(255.0, lo));
+            hi = std::max(0.0, std::min(255.0, hi));
+            q[k * 8 + s] = (uint8_t)lo;
+            q[(3 + k) * 8 + s] = (uint8_t)hi;
+        }
+    }
+}
+
+// Assign children to slots by centroid direction (octant order, bvh8.h).
+void assign_slots(const Box& node, const std::vector<Child>& kids, int slot_of[8]) {
+    double c[3];
+    for (int k = 0; k < 3; ++k) c[k] = 0.5 * (double(node.lo[k]) + double(node.hi[k]));
+    const int n = (int)kids.size();
+    double score[8][8];
+    for (int i = 0; i < n; ++i) {
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = 0.5 * (double(kids[i].box.lo[k]) + double(kids[i].box.hi[k])) - c[k];
+        for (int s = 0; s < 8; ++s) {
+            double v = 0;
+            for (int k = 0; k < 3; ++k) v += ((s >> k) & 1 ? 1.0 : -1.0) * d[k];
+            score[i][s] = v;
+        }
+    }
+    bool used_child[8] = {}, used_slot[8] = {};
+    for (int round = 0; round < n; ++round) {
+        double best = -INFINITY;
+        int bi = -1, bs = -1;
+        for (int i = 0; i < n; ++i) {
+            if (used_child[i]) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (used_slot[s]) continue;
+                if (score[i][s] > best || bi < 0) { best = score[i][s]; bi = i; bs = s; }
+            }
+        }
+        used_child[bi] = used_slot[bs] = true;
+        slot_of[bi] = bs;
+    }
+}
+
+void build_node(Impl& I, const std::vector<Child>& initial, int target, int depth);
+
+// Build the wide node at index `target` from binary node / range `root`.
+void build_from(Impl& I, const Child& root, int target, int depth) {
+    std::vector<Child> kids;
+    if (root.is_range()) {
+        if (root.count <= 3) kids.push_back(root);
+        else split_range(I, root, kids);
+    } else {
+        const BinNode& n = I.bn[root.bin];
+        children_of(I, n.l, kids);
+        children_of(I, n.r, kids);
+    }
+    build_node(I, kids, target, depth);
+}
+
+void build_node(Impl& I, const std::vector<Child>& initial, int target, int depth) {
+    if (depth > 200) fail("BVH deeper than 200 wide levels");
+    I.max_depth = std::max(I.max_depth, depth);
+    std::vector<Child> kids = initial;
+    // expand interior children (largest area first) while slots remain
+    for (;;) {
+        if (kids.size() >= 8) break;
+        int best = -1;
+        double best_area = -1;
+        for (size_t i = 0; i < kids.size(); ++i) {
+            if (kids[i].is_range()) continue;
+            double a = kids[i].box.area();
+            if (a > best_area) { best_area = a; best = (int)i; }
+        }
+        if (best < 0) break;
+        std::vector<Child> sub;
+        const BinNode& n = I.bn[kids[best].bin];
+        children_of(I, n.l, sub);
+        children_of(I, n.r, sub);
+        if (kids.size() - 1 + sub.size() > 8) break;
+        kids.erase(kids.begin() + best);
+        kids.insert(kids.end(), sub.begin(), sub.end());
+    }
+    if (kids.empty()) fail("empty BVH node");
+    Box nb;
+    nb.empty();
+    for (auto& k : kids) nb.grow(k.box);
+    int slot_of[8];
+    assign_slots(nb, kids, slot_of);
+    // internal children (interior binary nodes and oversized ranges), in slot order
+    std::vector<int> order(kids.size());
+    for (size_t i = 0; i < kids.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return slot_of[a] < slot_of[b]; });
+    uint8_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int imask = 0, num_internal = 0;
+    for (int i : order)
+        if (!kids[i].is_leaf_slot()) { imask |= 1 << slot_of[i]; ++num_internal; }
+    const int child_base = (int)I.nodes.size();
+    I.nodes.resize(I.nodes.size() + num_internal);
+    const int prim_base = I.tlas ? (int)I.insts.size() : (int)I.tris.size();
+    int prim_off = 0;
+    for (int i : order) {
+        const Child& c = kids[i];
+        const int s = slot_of[i];
+        if (!c.is_leaf_slot()) {
+            meta[s] = uint8_t((1 << 5) | (24 + s));
+            continue;
+        }
+        meta[s] = uint8_t((((1 << c.count) - 1) << 5) | prim_off);
+        prim_off += c.count;
+        if (I.tlas) {
+            auto it = I.blas_root_map.find(c.blas_root);
+            if (it == I.blas_root_map.end()) fail("TLAS leaf refers to an unbuilt BLAS root");
+            InstRef r;
+            r.blas_root = it->second;
+            r.instance = c.first;
+            r.material = c.material;
+            r.identity = I.inst_identity[c.first];
+            I.insts.push_back(r);
+        } else {
+            for (int t = c.first; t < c.first + c.count; ++t) {
+                WideTri wt;
+                const int32_t* vi = I.vidx + 3 * (size_t)t;
+                const float* a = I.verts + 4 * (size_t)vi[0];
+                const float* b = I.verts + 4 * (size_t)vi[1];
+                const float* d = I.verts + 4 * (size_t)vi[2];
+                for (int k = 0; k < 3; ++k) {
+                    wt.v0[k] = a[k];
+                    wt.e0[k] = b[k] - a[k];  // the shader's e0 = v1.xyz - v0.xyz (closest_hit.glsl:128)
+                    wt.e1[k] = d[k] - a[k];  // e1 = v2.xyz - v0.xyz
+                }
+                wt.e0[3] = wt.e1[3] = 0.0f;
+                wt.prim = t;
+                I.tris.push_back(wt);
+            }
+        }
+    }
+    if (prim_off > 24) fail("more than 24 primitives under one wide node");
+    quantise(nb, kids, slot_of, I.nodes[target], imask, child_base, prim_base, meta);
+    int j = 0;
+    for (int i : order) {
+        if (kids[i].is_leaf_slot()) continue;
+        build_from(I, kids[i], child_base + j, depth + 1);
+        ++j;
+    }
+}
+
+int build_root(Impl& I, int bin_root) {
+    const int target = (int)I.nodes.size();
+    I.nodes.emplace_back();
+    std::vector<Child> kids;
+    const BinNode& n = I.bn[bin_root];
+    if (n.leaf != 0) children_of(I, bin_root, kids);
+    else { children_of(I, n.l, kids); children_of(I, n.r, kids); }
+    if (kids.empty()) {
+        // an empty leaf: a wide node with no children never hits
+        std::memset(&I.nodes[target], 0, sizeof(WideNode));
+        return target;
+    }
+    if (kids.size() == 1 && kids[0].is_range() && kids[0].count > 3) {
+        std::vector<Child> sub;
+        split_range(I, kids[0], sub);
+        kids.swap(sub);
+    }
+    build_node(I, kids, target, 1);
+    return target;
+}
+
+void read_binary(Impl& I, const float* nodes, int n) {
+    I.bn.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const float* p = nodes + 9 * (size_t)i;
+        BinNode& b = I.bn[i];
+        for (int k = 0; k < 3; ++k) { b.lo[k] = p[k]; b.hi[k] = p[3 + k]; }
+        b.l = (int)p[6]; b.r = (int)p[7]; b.leaf = (int)p[8];
+    }
+}
+
+void collect_blas_roots(Impl& I, int top, std::vector<int>& roots) {
+    std::vector<int> stack{top};
+    std::vector<char> seen(I.bn.size(), 0);
+    while (!stack.empty()) {
+        int b = stack.back();
+        stack.pop_back();
+        if (b < 0 || b >= (int)I.bn.size()) fail("TLAS child index out of range");
+        if (seen[b]) fail("TLAS is not a tree");
+        seen[b] = 1;
+        const BinNode& n = I.bn[b];
+        if (n.leaf < 0) {
+            if (n.l < 0 || n.l >= (int)I.bn.size()) fail("BLAS root index out of range");
+            roots.push_back(n.l);
+        } else if (n.leaf == 0) {
+            stack.push_back(n.l);
+            stack.push_back(n.r);
+        } else {
+            fail("BLAS leaf inside the TLAS");
+        }
+    }
+}
+
+void publish(Impl& I, WideBVH* out) {
+    out->nodes = I.nodes.data();
+    out->num_nodes = (int)I.nodes.size();
+    out->tris = I.tris.data();
+    out->num_tris = (int)I.tris.size();
+    out->insts = I.insts.data();
+    out->num_inst_refs = (int)I.insts.size();
+    out->impl = &I;
+}
+
+void set_identity(Impl& I, const float* transforms, int num_instances) {
+    I.num_instances = num_instances;
+    I.inst_identity.assign(num_instances, 0);
+    for (int i = 0; i < num_instances; ++i) {
+        InstXf xf;
+        int id = 0;
+        ptgb_instance_xf(transforms + 16 * (size_t)i, &xf, &id);
+        I.inst_identity[i] = id;
+    }
+}
+
+void copy_err(const std::string& m, char* err, int n) {
+    if (err && n > 0) {
+        std::snprintf(err, n, "%s", m.c_str());
+    }
+}
+
+}  // namespace
+
+extern "C" void ptgb_instance_xf(const float* d16, InstXf* out, int* is_identity) {
+    double m[16];  // m[col*4+row] = data[col][row], the GLSL column-major matrix mat4(data rows)
+    for (int i = 0; i < 16; ++i) m[i] = d16[i];
+    int ident = 1;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r)
+            if (d16[c * 4 + r] != (c == r ? 1.0f : 0.0f)) ident = 0;
+    if (is_identity) *is_identity = ident;
+    // cofactor inverse, in double, rounded to float
+    double inv[16];
+    inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+    inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+    inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+    inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+    inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+    inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+    inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+    inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+    inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+    inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+    inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+    inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+    inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+    inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+    inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+    inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+    double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+    for (int i = 0; i < 16; ++i) out->inv[i] = float(inv[i] / det);
+    // mat3(transform): columns c = data[c][0..2]
+    double a[3][3];
+    for (int c = 0; c < 3; ++c) {
+        for (int r = 0; r < 3; ++r) {
+            a[c][r] = d16[c * 4 + r];
+            out->m3[c * 4 + r] = d16[c * 4 + r];
+        }
+        out->m3[c * 4 + 3] = 0.0f;
+    }
+    const double A = a[0][0], B = a[1][0], C = a[2][0];
+    const double D = a[0][1], E = a[1][1], F = a[2][1];
+    const double G = a[0][2], H = a[1][2], I = a[2][2];
+    const double cof[3][3] = {{E * I - F * H, -(D * I - F * G), D * H - E * G},
+                              {-(B * I - C * H), A * I - C * G, -(A * H - B * G)},
+                              {B * F - C * E, -(A * F - C * D), A * E - B * D}};
+    const double d3 = A * cof[0][0] + B * cof[0][1] + C * cof[0][2];
+    // transpose(inverse(m3)): element (row r, col c) = cof[r][c] / det
+    for (int c = 0; c < 3; ++c) {
+        for (int r = 0; r < 3; ++r) out->nrm[c * 4 + r] = float(cof[r][c] / d3);
+        out->nrm[c * 4 + 3] = 0.0f;
+    }
+}
+
+extern "C" int ptgb_build_wide(const float* bvh_nodes, int num_bvh_nodes, int top_level_index,
+                               const int32_t* vert_indices, int num_tris, const float* vertices_uvx, int num_vertices,
+                               const float* transforms, int num_instances, WideBVH* out, char* err, int err_size) {
+    Impl* I = new Impl;
+    try {
+        if (!bvh_nodes || num_bvh_nodes <= 0) fail("no BVH nodes");
+        if (top_level_index < 0 || top_level_index >= num_bvh_nodes) fail("top_level_index out of range");
+        read_binary(*I, bvh_nodes, num_bvh_nodes);
+        I->vidx = vert_indices;
+        I->verts = vertices_uvx;
+        I->num_tris = num_tris;
+        I->num_vertices = num_vertices;
+        set_identity(*I, transforms, num_instances);
+        std::vector<int> roots;
+        collect_blas_roots(*I, top_level_index, roots);
+        I->tlas = false;
+        for (int r : roots) {
+            if (I->blas_root_map.count(r)) continue;
+            if (I->bn[r].leaf < 0) fail("BLAS root is a TLAS leaf");
+            I->blas_root_map[r] = build_root(*I, r);
+        }
+        I->blas_node_count = (int)I->nodes.size();
+        I->blas_tri_count = (int)I->tris.size();
+        out->blas_depth = I->max_depth;
+        I->max_depth = 0;
+        I->tlas = true;
+        out->tlas_first_node = (int)I->nodes.size();
+        out->tlas_root = build_root(*I, top_level_index);
+        out->tlas_depth = I->max_depth;
+        publish(*I, out);
+        return PT_OK;
+    } catch (const BuildError& e) {
+        copy_err(e.msg, err, err_size);
+        delete I;
+        out->impl = nullptr;
+        return PT_ERR_INVALID_ARG;
+    } catch (const std::bad_alloc&) {
+        copy_err("host allocation failed in BVH collapse", err, err_size);
+        delete I;
+        out->impl = nullptr;
+        return PT_ERR_OUT_OF_MEMORY;
+    }
+}
+
+extern "C" int ptgb_rebuild_tlas(WideBVH* out, const float* bvh_nodes, int num_bvh_nodes, int top_level_index,
+                                 const float* transforms, int num_instances, char* err, int err_size) {
+    Impl* I = static_cast<Impl*>(out->impl);
+    if (!I) { copy_err("no BVH to update", err, err_size); return PT_ERR_INVALID_ARG; }
+    try {
+        if (top_level_index < 0 || top_level_index >= num_bvh_nodes) fail("top_level_index out of range");
+        // the BLAS part of the binary array is unchanged (Scene::RebuildInstances
+        // rewrites only the TLAS slice, Scene.cpp:200-214)
+        if ((int)I->bn.size() < num_bvh_nodes) I->bn.resize(num_bvh_nodes);
+        for (int i = top_level_index; i < num_bvh_nodes; ++i) {
+            const float* p = bvh_nodes + 9 * (size_t)i;
+            BinNode& b = I->bn[i];
+            for (int k = 0; k < 3; ++k) { b.lo[k] = p[k]; b.hi[k] = p[3 + k]; }
+            b.l = (int)p[6]; b.r = (int)p[7]; b.leaf = (int)p[8];
+        }
+        set_identity(*I, transforms, num_instances);
+        I->nodes.resize(I->blas_node_count);
+        I->tris.resize(I->blas_tri_count);
+        I->insts.clear();
+        std::vector<int> roots;
+        collect_blas_roots(*I, top_level_index, roots);
+        for (int r : roots)
+            if (!I->blas_root_map.count(r)) fail("TLAS refers to a BLAS that was not in the original scene");
+        I->tlas = true;
+        I->max_depth = 0;
+        out->tlas_first_node = (int)I->nodes.size();
+        out->tlas_root = build_root(*I, top_level_index);
+        out->tlas_depth = I->max_depth;
+        publish(*I, out);
+        return PT_OK;
+    } catch (const BuildError& e) {
+        copy_err(e.msg, err, err_size);
+        return PT_ERR_INVALID_ARG;
+    }
+}
+
+extern "C" void ptgb_free_wide(WideBVH* out) {
+    delete static_cast<Impl*>(out->impl);
+    out->impl = nullptr;
+    out->nodes = nullptr;
+    out->tris = nullptr;
+    out->insts = nullptr;
+    out->num_nodes = out->num_tris = out->num_inst_refs = 0;
+}

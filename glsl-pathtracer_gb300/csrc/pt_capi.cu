@@ -1,0 +1,557 @@
+// pt_capi.cu - the C ABI of include/pt_cuda.h: one context per renderer,
+// owning the device copies of the scene, the accumulation buffer and a
+// CUDA stream.  Replaces GLSLPT::Renderer's GL resource management
+// (src/core/Renderer.cpp:41-249, 619-811).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pt_cuda.h"
+#include "bvh8.h"
+#include "pt_device.cuh"
+#include "pt_params.h"
+
+using namespace ptgb;
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_err(cudaError_t e, const char* what) {
+    const int code = e == cudaErrorMemoryAllocation ? PT_ERR_OUT_OF_MEMORY : PT_ERR_CUDA;
+    return set_err(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_err(e_, #call);    \
+    } while (0)
+
+template <class T> struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        free();
+        n = count;
+        if (!count) return cudaSuccess;
+        return cudaMalloc((void**)&p, count * sizeof(T));
+    }
+    cudaError_t upload(const void* src, size_t count, cudaStream_t s) {
+        if (count != n) {
+            cudaError_t e = alloc(count);
+            if (e != cudaSuccess) return e;
+        }
+        if (!count) return cudaSuccess;
+        return cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, s);
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct pt_context {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    pt_render_options opts{};
+    pt_camera cam{};
+    int integrator = PT_INTEGRATOR_MEGAKERNEL;
+    uint32_t scene_flags = 0;  // F_ALPHA_TEST / F_MEDIUM / F_LIGHTS from the scene
+    bool has_env = false;
+    WideBVH bvh{};
+    std::vector<float> bin_nodes;  // host copy of the binary BVH (TLAS updates)
+    int top_level_index = 0;
+    int num_tris = 0, num_vertices = 0, num_materials = 0, num_instances = 0, num_lights = 0;
+    int env_w = 0, env_h = 0;
+    float env_total = 0.0f;
+    DevBuf<WideNode> nodes;
+    DevBuf<WideTri> tris;
+    DevBuf<InstRef> insts;
+    DevBuf<InstXf> xf;
+    DevBuf<int32_t> vidx;
+    DevBuf<float4> verts, norms, mats, lights, env;
+    DevBuf<float> cdf;
+    DevBuf<float4> accum;
+    DevBuf<float4> snapshot;
+    DevBuf<uchar4> ldr;
+    DevBuf<unsigned long long> counters;
+    DevBuf<int> status;
+    pt_stats last{};
+};
+
+namespace {
+
+uint32_t option_flags(const pt_context* c) {
+    const pt_render_options& o = c->opts;
+    uint32_t f = c->scene_flags;
+    if (o.enable_rr) f |= F_RR;
+    if (o.enable_uniform_light) f |= F_UNIFORM_LIGHT;
+    if (o.hide_emitters) f |= F_HIDE_EMITTERS;
+    if (o.enable_background || o.transparent_background) f |= F_BACKGROUND;
+    if (o.enable_roughness_mollification) f |= F_MOLLIFY;
+    if (o.enable_envmap && c->has_env && !o.enable_uniform_light) f |= F_ENVMAP;
+    if (o.enable_volume_mis) f |= F_VOL_MIS;
+    return f;
+}
+
+Params make_params(const pt_context* c) {
+    Params p{};
+    p.nodes = reinterpret_cast<const uint4*>(c->nodes.p);
+    p.tris = reinterpret_cast<const float4*>(c->tris.p);
+    p.insts = reinterpret_cast<const int4*>(c->insts.p);
+    p.xf = reinterpret_cast<const float4*>(c->xf.p);
+    p.tlas_root = c->bvh.tlas_root;
+    p.vidx = c->vidx.p;
+    p.verts = c->verts.p;
+    p.norms = c->norms.p;
+    p.mats = c->mats.p;
+    p.lights = c->lights.p;
+    p.num_lights = c->num_lights;
+    p.num_materials = c->num_materials;
+    p.env = c->env.p;
+    p.cdf = c->cdf.p;
+    p.env_w = c->env_w;
+    p.env_h = c->env_h;
+    p.env_total = c->env_total;
+    p.env_intensity = c->opts.envmap_intensity;
+    p.env_rot = c->opts.envmap_rot / 360.0f;  // Renderer.cpp:778
+    p.flags = option_flags(c);
+    p.max_depth = c->opts.max_depth;
+    p.rr_depth = c->opts.rr_depth;
+    for (int i = 0; i < 3; ++i) {
+        p.uniform_light[i] = c->opts.uniform_light_col[i];
+        p.cam_pos[i] = c->cam.position[i];
+        p.cam_up[i] = c->cam.up[i];
+        p.cam_right[i] = c->cam.right[i];
+        p.cam_fwd[i] = c->cam.forward[i];
+    }
+    p.mollify_amt = c->opts.roughness_mollification_amt;
+    p.cam_fov = c->cam.fov;
+    p.cam_focal = c->cam.focal_dist;
+    p.cam_aperture = c->cam.aperture;
+    p.width = c->opts.render_width;
+    p.height = c->opts.render_height;
+    p.tile_w = c->opts.tile_width;
+    p.tile_h = c->opts.tile_height;
+    p.ntx = (p.width + p.tile_w - 1) / p.tile_w;
+    p.nty = (p.height + p.tile_h - 1) / p.tile_h;
+    p.accum = c->accum.p;
+    p.counters = c->counters.p;
+    p.status = c->status.p;
+    return p;
+}
+
+int check_options(const pt_render_options* o) {
+    if (!o) return set_err(PT_ERR_INVALID_ARG, "options is NULL");
+    if (o->render_width <= 0 || o->render_height <= 0 || o->render_width > 32768 || o->render_height > 32768)
+        return set_err(PT_ERR_INVALID_ARG, "render resolution out of range");
+    if (o->tile_width <= 0 || o->tile_height <= 0) return set_err(PT_ERR_INVALID_ARG, "tile size must be positive");
+    if (o->max_depth < 0 || o->max_depth > 1024) return set_err(PT_ERR_INVALID_ARG, "max_depth out of range");
+    return PT_OK;
+}
+
+int upload_instances(pt_context* c, const float* transforms, int n) {
+    std::vector<InstXf> xf(n);
+    for (int i = 0; i < n; ++i) {
+        int ident = 0;
+        ptgb_instance_xf(transforms + 16 * (size_t)i, &xf[i], &ident);
+    }
+    CK(c->xf.upload(xf.data(), xf.size(), c->stream));
+    return PT_OK;
+}
+
+int upload_bvh(pt_context* c) {
+    CK(c->nodes.upload(c->bvh.nodes, c->bvh.num_nodes, c->stream));
+    CK(c->tris.upload(c->bvh.tris, c->bvh.num_tris, c->stream));
+    CK(c->insts.upload(c->bvh.insts, c->bvh.num_inst_refs, c->stream));
+    if (c->bvh.tlas_depth + c->bvh.blas_depth > kStackSize)
+        return set_err(PT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" +
+                                               std::to_string(c->bvh.tlas_depth + c->bvh.blas_depth) + " levels)");
+    return PT_OK;
+}
+
+int upload_envmap(pt_context* c, const float* rgb, const float* cdf, int w, int h, float total) {
+    c->has_env = rgb != nullptr && cdf != nullptr && w > 0 && h > 0;
+    if (!c->has_env) {
+        c->env.free();
+        c->cdf.free();
+        c->env_w = c->env_h = 0;
+        return PT_OK;
+    }
+    std::vector<float4> px((size_t)w * h);
+    for (size_t i = 0; i < px.size(); ++i) px[i] = make_float4(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], 0.0f);
+    CK(c->env.upload(px.data(), px.size(), c->stream));
+    CK(c->cdf.upload(cdf, (size_t)w * h, c->stream));
+    c->env_w = w;
+    c->env_h = h;
+    c->env_total = total;
+    CK(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+int alloc_accum(pt_context* c) {
+    const size_t n = (size_t)c->opts.render_width * c->opts.render_height;
+    if (c->accum.n != n) {
+        CK(c->accum.alloc(n));
+        c->ldr.free();
+        c->snapshot.free();
+    }
+    CK(cudaMemsetAsync(c->accum.p, 0, n * sizeof(float4), c->stream));
+    return PT_OK;
+}
+
+uint32_t scene_flags_of(const float* mats, int nm, int nl) {
+    uint32_t f = 0;
+    if (nl > 0) f |= F_LIGHTS;
+    for (int i = 0; i < nm; ++i) {
+        if ((int)mats[32 * i + 29] != ALPHA_MODE_OPAQUE) f |= F_ALPHA_TEST;  // Renderer.cpp:443-450
+        if ((int)mats[32 * i + 18] != MEDIUM_NONE) f |= F_MEDIUM;            // Renderer.cpp:455-461
+    }
+    return f;
+}
+
+int check_materials(const float* mats, int nm) {
+    for (int i = 0; i < nm; ++i)
+        for (int k = 24; k < 28; ++k)
+            if ((int)mats[32 * i + k] >= 0)
+                return set_err(PT_ERR_UNSUPPORTED, "material " + std::to_string(i) +
+                                                       " uses a texture map; texture maps are not supported yet");
+    return PT_OK;
+}
+
+int begin_launch(pt_context* c) {
+    CK(cudaMemsetAsync(c->counters.p, 0, 3 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    return PT_OK;
+}
+
+int end_launch(pt_context* c) {
+    CK(cudaEventRecord(c->ev1, c->stream));
+    c->timed = true;
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_last_error(char* buf, size_t size) {
+    if (!buf || !size) return PT_ERR_INVALID_ARG;
+    std::snprintf(buf, size, "%s", g_err.c_str());
+    return PT_OK;
+}
+
+int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** out) {
+    if (!d || !out) return set_err(PT_ERR_INVALID_ARG, "scene or output pointer is NULL");
+    *out = nullptr;
+    if (int rc = check_options(o)) return rc;
+    if (!d->bvh_nodes || d->num_bvh_nodes <= 0 || !d->vert_indices || d->num_tris < 0 || !d->vertices_uvx ||
+        !d->normals_uvy || d->num_vertices <= 0 || !d->transforms || d->num_instances <= 0 || !d->materials ||
+        d->num_materials <= 0 || d->num_lights < 0 || (d->num_lights > 0 && !d->lights))
+        return set_err(PT_ERR_INVALID_ARG, "incomplete scene description");
+    if (d->num_textures > 0) return set_err(PT_ERR_UNSUPPORTED, "texture maps are not supported yet");
+    if (int rc = check_materials(d->materials, d->num_materials)) return rc;
+    for (int i = 0; i < d->num_lights; ++i) {
+        int type = (int)d->lights[15 * i + 14];
+        if (type < 0 || type > 2) return set_err(PT_ERR_INVALID_ARG, "unknown light type");
+    }
+    pt_context* c = new pt_context;
+    c->opts = *o;
+    int rc = PT_OK;
+    do {
+        cudaError_t e = cudaGetDevice(&c->device);
+        if (e != cudaSuccess) { rc = cuda_err(e, "cudaGetDevice"); break; }
+        e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { rc = cuda_err(e, "cudaStreamCreate"); break; }
+        c->stream = c->own_stream;
+        if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+            rc = cuda_err(e, "cudaEventCreate");
+            break;
+        }
+        char msg[512] = {0};
+        rc = ptgb_build_wide(d->bvh_nodes, d->num_bvh_nodes, d->top_level_index, d->vert_indices, d->num_tris,
+                             d->vertices_uvx, d->num_vertices, d->transforms, d->num_instances, &c->bvh, msg,
+                             sizeof msg);
+        if (rc) { set_err(rc, std::string("BVH: ") + msg); break; }
+        for (int i = 0; i < c->bvh.num_inst_refs; ++i) {
+            if (c->bvh.insts[i].material < 0 || c->bvh.insts[i].material >= d->num_materials) {
+                rc = set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
+                break;
+            }
+        }
+        if (rc) break;
+        c->bin_nodes.assign(d->bvh_nodes, d->bvh_nodes + 9 * (size_t)d->num_bvh_nodes);
+        c->top_level_index = d->top_level_index;
+        c->num_tris = d->num_tris;
+        c->num_vertices = d->num_vertices;
+        c->num_materials = d->num_materials;
+        c->num_instances = d->num_instances;
+        c->num_lights = d->num_lights;
+        c->scene_flags = scene_flags_of(d->materials, d->num_materials, d->num_lights);
+        if ((rc = upload_bvh(c))) break;
+        if ((rc = upload_instances(c, d->transforms, d->num_instances))) break;
+        if ((e = c->vidx.upload(d->vert_indices, 3 * (size_t)d->num_tris, c->stream)) != cudaSuccess ||
+            (e = c->verts.upload(d->vertices_uvx, d->num_vertices, c->stream)) != cudaSuccess ||
+            (e = c->norms.upload(d->normals_uvy, d->num_vertices, c->stream)) != cudaSuccess ||
+            (e = c->mats.upload(d->materials, 8 * (size_t)d->num_materials, c->stream)) != cudaSuccess) {
+            rc = cuda_err(e, "scene upload");
+            break;
+        }
+        std::vector<float4> L(4 * (size_t)std::max(1, d->num_lights));
+        for (int i = 0; i < d->num_lights; ++i) {
+            const float* s = d->lights + 15 * (size_t)i;  // position, emission, u, v, (radius, area, type)
+            L[4 * i + 0] = make_float4(s[0], s[1], s[2], s[12]);
+            L[4 * i + 1] = make_float4(s[3], s[4], s[5], s[13]);
+            L[4 * i + 2] = make_float4(s[6], s[7], s[8], s[14]);
+            L[4 * i + 3] = make_float4(s[9], s[10], s[11], 0.0f);
+        }
+        if ((e = c->lights.upload(L.data(), L.size(), c->stream)) != cudaSuccess) { rc = cuda_err(e, "lights"); break; }
+        if ((rc = upload_envmap(c, d->envmap_rgb, d->envmap_cdf, d->envmap_width, d->envmap_height,
+                                d->envmap_total_sum)))
+            break;
+        if ((e = c->counters.alloc(3)) != cudaSuccess || (e = c->status.alloc(1)) != cudaSuccess) {
+            rc = cuda_err(e, "counters");
+            break;
+        }
+        if ((rc = alloc_accum(c))) break;
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) { rc = cuda_err(e, "upload"); break; }
+    } while (0);
+    if (rc) {
+        pt_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return PT_OK;
+}
+
+int pt_destroy(pt_context* c) {
+    if (!c) return PT_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->vidx.free(); c->verts.free();
+    c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
+    c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    ptgb_free_wide(&c->bvh);
+    delete c;
+    return PT_OK;
+}
+
+int pt_set_stream(pt_context* c, void* s) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = s ? (cudaStream_t)s : c->own_stream;
+    return PT_OK;
+}
+
+int pt_set_camera(pt_context* c, const pt_camera* cam) {
+    if (!c || !cam) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    c->cam = *cam;
+    return PT_OK;
+}
+
+int pt_set_options(pt_context* c, const pt_render_options* o) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    if (int rc = check_options(o)) return rc;
+    const bool resize = o->render_width != c->opts.render_width || o->render_height != c->opts.render_height ||
+                        o->tile_width != c->opts.tile_width || o->tile_height != c->opts.tile_height;
+    c->opts = *o;
+    if (resize) return alloc_accum(c);
+    return PT_OK;
+}
+
+int pt_set_integrator(pt_context* c, int32_t integrator) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    if (integrator != PT_INTEGRATOR_MEGAKERNEL && integrator != PT_INTEGRATOR_WAVEFRONT)
+        return set_err(PT_ERR_INVALID_ARG, "unknown integrator");
+    c->integrator = integrator;
+    return PT_OK;
+}
+
+int pt_update_instances(pt_context* c, const float* transforms, int32_t num_instances, const float* materials,
+                        int32_t num_materials, const float* tlas_nodes, int32_t num_tlas_nodes) {
+    if (!c || !transforms || num_instances <= 0 || !tlas_nodes || num_tlas_nodes <= 0)
+        return set_err(PT_ERR_INVALID_ARG, "invalid instance update");
+    if (materials) {
+        if (num_materials <= 0) return set_err(PT_ERR_INVALID_ARG, "num_materials must be positive");
+        if (int rc = check_materials(materials, num_materials)) return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->bin_nodes.resize(9 * (size_t)(c->top_level_index + num_tlas_nodes));
+    std::memcpy(c->bin_nodes.data() + 9 * (size_t)c->top_level_index, tlas_nodes, 9 * sizeof(float) * num_tlas_nodes);
+    char msg[512] = {0};
+    int rc = ptgb_rebuild_tlas(&c->bvh, c->bin_nodes.data(), c->top_level_index + num_tlas_nodes, c->top_level_index,
+                               transforms, num_instances, msg, sizeof msg);
+    if (rc) return set_err(rc, std::string("TLAS: ") + msg);
+    const int nm = materials ? num_materials : c->num_materials;
+    for (int i = 0; i < c->bvh.num_inst_refs; ++i)
+        if (c->bvh.insts[i].material < 0 || c->bvh.insts[i].material >= nm)
+            return set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
+    c->num_instances = num_instances;
+    if ((rc = upload_bvh(c))) return rc;
+    if ((rc = upload_instances(c, transforms, num_instances))) return rc;
+    if (materials) {
+        CK(c->mats.upload(materials, 8 * (size_t)num_materials, c->stream));
+        c->num_materials = num_materials;
+        c->scene_flags = scene_flags_of(materials, num_materials, c->num_lights);
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+int pt_update_envmap(pt_context* c, const float* rgb, const float* cdf, int32_t w, int32_t h, float total) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    if (rgb && (w <= 0 || h <= 0 || !cdf)) return set_err(PT_ERR_INVALID_ARG, "invalid envmap");
+    CK(cudaStreamSynchronize(c->stream));
+    return upload_envmap(c, rgb, cdf, w, h, total);
+}
+
+int pt_clear_accum(pt_context* c) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    CK(cudaMemsetAsync(c->accum.p, 0, c->accum.n * sizeof(float4), c->stream));
+    return PT_OK;
+}
+
+int pt_render_tile(pt_context* c, int32_t tx, int32_t ty, int32_t frame) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    const pt_render_options& o = c->opts;
+    const int ntx = (o.render_width + o.tile_width - 1) / o.tile_width;
+    const int nty = (o.render_height + o.tile_height - 1) / o.tile_height;
+    if (tx < 0 || ty < 0 || tx >= ntx || ty >= nty) return set_err(PT_ERR_INVALID_ARG, "tile out of range");
+    if (frame < 0) return set_err(PT_ERR_INVALID_ARG, "negative frame number");
+    RenderWork w;
+    w.x0 = tx * o.tile_width;
+    w.y0 = ty * o.tile_height;
+    w.w = std::min(o.tile_width, o.render_width - w.x0);
+    w.h = std::min(o.tile_height, o.render_height - w.y0);
+    w.first_pass = 0;
+    w.num_passes = 1;
+    w.tile_frame = frame;
+    w.tile_x = tx;
+    w.tile_y = ty;
+    if (int rc = begin_launch(c)) return rc;
+    CK(launch_render(make_params(c), w, c->integrator, c->stream));
+    return end_launch(c);
+}
+
+int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    if (first_pass < 0 || num_passes < 0) return set_err(PT_ERR_INVALID_ARG, "negative pass range");
+    RenderWork w;
+    w.x0 = w.y0 = 0;
+    w.w = c->opts.render_width;
+    w.h = c->opts.render_height;
+    w.first_pass = first_pass;
+    w.num_passes = num_passes;
+    w.tile_frame = -1;
+    w.tile_x = w.tile_y = 0;
+    if (int rc = begin_launch(c)) return rc;
+    CK(launch_render(make_params(c), w, c->integrator, c->stream));
+    return end_launch(c);
+}
+
+int pt_get_accum(pt_context* c, float* host) {
+    if (!c || !host) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    CK(cudaMemcpyAsync(host, c->accum.p, c->accum.n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+int pt_snapshot_accum(pt_context* c) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    if (c->snapshot.n != c->accum.n) CK(c->snapshot.alloc(c->accum.n));
+    CK(cudaMemcpyAsync(c->snapshot.p, c->accum.p, c->accum.n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    return PT_OK;
+}
+
+int pt_get_output(pt_context* c, int32_t num_samples, int32_t from_snapshot, uint8_t* host) {
+    if (!c || !host || num_samples <= 0) return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    if (from_snapshot && c->snapshot.n != c->accum.n) return set_err(PT_ERR_INVALID_ARG, "no snapshot taken");
+    if (c->ldr.n != c->accum.n) CK(c->ldr.alloc(c->accum.n));
+    const pt_render_options& o = c->opts;
+    Params p = make_params(c);
+    if (from_snapshot) p.accum = c->snapshot.p;
+    CK(launch_tonemap(p, num_samples, o.enable_tonemap, o.enable_aces, o.simple_aces_fit,
+                      o.enable_background, o.transparent_background, o.background_col, (unsigned char*)c->ldr.p,
+                      c->stream));
+    CK(cudaMemcpyAsync(host, c->ldr.p, c->ldr.n * sizeof(uchar4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+int pt_trace_rays(pt_context* c, const pt_ray* rays, int32_t n, pt_hit* hits) {
+    if (!c || n < 0 || (n && (!rays || !hits))) return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    if (!n) return PT_OK;
+    DevBuf<pt_ray> dr;
+    DevBuf<pt_hit> dh;
+    CK(dr.upload(rays, n, c->stream));
+    CK(dh.alloc(n));
+    CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+    CK(launch_trace_closest(make_params(c), dr.p, n, dh.p, c->stream));
+    CK(cudaMemcpyAsync(hits, dh.p, n * sizeof(pt_hit), cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    dr.free();
+    dh.free();
+    if (st) return set_err(st, "traversal stack overflow");
+    return PT_OK;
+}
+
+int pt_trace_shadow(pt_context* c, const pt_ray* rays, const float* maxd, int32_t n, uint8_t* occ) {
+    if (!c || n < 0 || (n && (!rays || !maxd || !occ))) return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    if (!n) return PT_OK;
+    DevBuf<pt_ray> dr;
+    DevBuf<float> dm;
+    DevBuf<uint8_t> dout;
+    CK(dr.upload(rays, n, c->stream));
+    CK(dm.upload(maxd, n, c->stream));
+    CK(dout.alloc(n));
+    CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
+    CK(launch_trace_shadow(make_params(c), dr.p, dm.p, n, dout.p, c->stream));
+    CK(cudaMemcpyAsync(occ, dout.p, n, cudaMemcpyDeviceToHost, c->stream));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    dr.free();
+    dm.free();
+    dout.free();
+    if (st) return set_err(st, "traversal stack overflow");
+    return PT_OK;
+}
+
+int pt_get_stats(pt_context* c, pt_stats* s) {
+    if (!c || !s) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    unsigned long long cnt[3] = {0, 0, 0};
+    int st = 0;
+    CK(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.0f;
+    if (c->timed) CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    s->closest_rays = cnt[0];
+    s->shadow_rays = cnt[1];
+    s->paths = cnt[2];
+    s->kernel_ms = ms;
+    s->status = st;
+    return PT_OK;
+}
+
+}  // extern "C"

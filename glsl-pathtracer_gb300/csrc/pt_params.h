@@ -1,0 +1,70 @@
+// pt_params.h - launch parameters shared by the host context (pt_capi.cu)
+// and the kernels (pt_kernels.cu).  Everything the reference passes as
+// textures and uniforms (common/uniforms.glsl:25-53, globals.glsl:141) is a
+// device pointer or a value here, passed by value at each launch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ptgb {
+
+// Traversal stack entries per thread (node groups of the wide BVH; one per
+// wide level on the current path, TLAS + BLAS).
+constexpr int kStackSize = 48;
+
+struct Params {
+    // acceleration structure (bvh8.h)
+    const uint4* nodes;     // WideNode, 5 x uint4
+    const float4* tris;     // WideTri, 3 x float4
+    const int4* insts;      // InstRef
+    const float4* xf;       // InstXf, 10 x float4 per instance
+    int tlas_root;
+    // reference arrays used for shading
+    const int* vidx;        // Indices, 3 x int32 per triangle
+    const float4* verts;    // verticesUVX
+    const float4* norms;    // normalsUVY
+    const float4* mats;     // Material, 8 x float4
+    const float4* lights;   // Light repacked as 4 x float4
+    int num_lights;
+    int num_materials;
+    // environment map (RGB padded to float4) and its CDF
+    const float4* env;
+    const float* cdf;
+    int env_w, env_h;
+    float env_total, env_intensity, env_rot;
+    // options
+    uint32_t flags;         // F_* bits (pt_device.cuh)
+    int max_depth, rr_depth;
+    float uniform_light[3];
+    float mollify_amt;
+    // camera (GLSLPT::Camera, globals.glsl:83-92)
+    float cam_pos[3], cam_up[3], cam_right[3], cam_fwd[3];
+    float cam_fov, cam_focal, cam_aperture;
+    // frame
+    int width, height, tile_w, tile_h, ntx, nty;
+    // output / bookkeeping
+    float4* accum;
+    unsigned long long* counters;  // [0] closest-hit queries, [1] shadow queries, [2] paths
+    int* status;                   // PT_OK or a PT_ERR_* code set by the kernels
+};
+
+// Work description of one render launch.
+struct RenderWork {
+    int x0, y0, w, h;       // pixel rectangle (full frame or one tile, clipped)
+    int first_pass, num_passes;
+    int tile_frame;         // >= 0: frame number of a single tile launch (pt_render_tile)
+    int tile_x, tile_y;     // tile of a single-tile launch
+};
+
+}  // namespace ptgb
+
+// kernel launchers (pt_kernels.cu)
+namespace ptgb {
+cudaError_t launch_render(const Params& p, const RenderWork& w, int integrator, cudaStream_t s);
+cudaError_t launch_trace_closest(const Params& p, const void* rays, int n, void* hits, cudaStream_t s);
+cudaError_t launch_trace_shadow(const Params& p, const void* rays, const float* maxd, int n, unsigned char* occ,
+                                cudaStream_t s);
+cudaError_t launch_tonemap(const Params& p, int num_samples, int enable_tonemap, int enable_aces, int simple_aces,
+                           int background, int transparent, const float* bg, unsigned char* out, cudaStream_t s);
+}  // namespace ptgb

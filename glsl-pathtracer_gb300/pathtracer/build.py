@@ -1,0 +1,73 @@
+"""Build of libptgb.so (the CUDA path) from csrc/, in-tree.
+
+nvcc compiles each translation unit for sm_103a only
+(-gencode arch=compute_103a,code=sm_103a) in parallel; the host-side BVH
+collapse is plain C++.  No cmake, no torch extension machinery.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+from .capi import PKG_DIR
+
+CSRC = os.path.join(PKG_DIR, "csrc")
+OBJ = os.path.join(CSRC, "_build")
+LIB = os.path.join(CSRC, "libptgb.so")
+
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
+CU_SOURCES = ["pt_kernels.cu", "pt_capi.cu"]
+CPP_SOURCES = ["bvh8_build.cpp", "cuda_renderer.cpp"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
+    os.makedirs(OBJ, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(os.path.dirname(PKG_DIR), "include", "pt_cuda.h"))
+    nv = nvcc()
+    jobs = []
+    objs = []
+    for src in CU_SOURCES + CPP_SOURCES:
+        path = os.path.join(CSRC, src)
+        if not os.path.exists(path):
+            continue
+        obj = os.path.join(OBJ, src + ".o")
+        objs.append(obj)
+        if not force and not _stale(obj, [path] + headers):
+            continue
+        if src.endswith(".cu"):
+            cmd = [nv] + NVCC_FLAGS + (extra_flags or []) + ["-c", path, "-o", obj]
+        else:
+            cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I/usr/local/cuda/include", "-c", path, "-o", obj]
+        jobs.append(cmd)
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out.strip():
+                print(out)
+    if force or _stale(LIB, objs):
+        _run([nv, "-shared", "-gencode", "arch=compute_103a,code=sm_103a"] + objs + ["-o", LIB, "-lcudart"])
+    return LIB

@@ -147,15 +147,16 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_render_tile.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.pt_render_passes.argtypes = [P, C.c_int32, C.c_int32]
     lib.pt_get_accum.argtypes = [P, _f]
-    lib.pt_get_output.argtypes = [P, C.c_int32, _u8]
+    lib.pt_snapshot_accum.argtypes = [P]
+    lib.pt_get_output.argtypes = [P, C.c_int32, C.c_int32, _u8]
     lib.pt_trace_rays.argtypes = [P, C.POINTER(pt_ray), C.c_int32, C.POINTER(pt_hit)]
     lib.pt_trace_shadow.argtypes = [P, C.POINTER(pt_ray), _f, C.c_int32, _u8]
     lib.pt_get_stats.argtypes = [P, C.POINTER(pt_stats)]
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in ("pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_passes",
-                 "pt_get_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow", "pt_get_stats",
-                 "pt_last_error"):
+                 "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
+                 "pt_get_stats", "pt_last_error"):
         getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib
@@ -165,7 +166,8 @@ def load_library(path: str | None = None) -> C.CDLL:
 HEADER_SYMBOLS = [
     "pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
     "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_passes",
-    "pt_get_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow", "pt_get_stats", "pt_last_error",
+    "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow", "pt_get_stats",
+    "pt_last_error",
 ]
 
 

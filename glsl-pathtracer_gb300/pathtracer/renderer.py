@@ -1,0 +1,124 @@
+"""Python-side handle on one libptgb context (the CUDA path).
+
+Thin: every method is one C ABI call (include/pt_cuda.h) plus numpy
+marshalling.  Used by the tests, smoke() and bench.py; a C++ program uses
+CudaRenderer (csrc/cuda_renderer.h) or the C ABI directly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .scene import SceneData
+
+HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), ("prim_id", np.int32),
+                      ("inst_id", np.int32)])
+
+
+class GpuRenderer:
+    def __init__(self, scene: SceneData, options: capi.pt_render_options | None = None, **overrides):
+        self.lib = capi.load_library()
+        self.scene = scene
+        self.options = options if options is not None else scene.render_options(**overrides)
+        self._desc = scene.desc()
+        self.ctx = C.c_void_p()
+        capi.check(self.lib, self.lib.pt_create(C.byref(self._desc), C.byref(self.options), C.byref(self.ctx)))
+        self.set_camera(scene.pt_camera())
+
+    # ------------------------------------------------------------------
+    @property
+    def width(self):
+        return self.options.render_width
+
+    @property
+    def height(self):
+        return self.options.render_height
+
+    def _ck(self, rc):
+        capi.check(self.lib, rc)
+
+    def set_camera(self, cam: capi.pt_camera):
+        self.camera = cam
+        self._ck(self.lib.pt_set_camera(self.ctx, C.byref(cam)))
+
+    def set_options(self, options: capi.pt_render_options):
+        self.options = options
+        self._ck(self.lib.pt_set_options(self.ctx, C.byref(options)))
+
+    def set_stream(self, stream_ptr: int | None):
+        self._ck(self.lib.pt_set_stream(self.ctx, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def set_integrator(self, which: int):
+        self._ck(self.lib.pt_set_integrator(self.ctx, which))
+
+    def clear(self):
+        self._ck(self.lib.pt_clear_accum(self.ctx))
+
+    def render_passes(self, first_pass: int, num_passes: int):
+        self._ck(self.lib.pt_render_passes(self.ctx, first_pass, num_passes))
+
+    def render_tile(self, tx: int, ty: int, frame: int):
+        self._ck(self.lib.pt_render_tile(self.ctx, tx, ty, frame))
+
+    def accum(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.float32)
+        self._ck(self.lib.pt_get_accum(self.ctx, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def snapshot(self):
+        self._ck(self.lib.pt_snapshot_accum(self.ctx))
+
+    def output(self, num_samples: int, from_snapshot: bool = False) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        self._ck(self.lib.pt_get_output(self.ctx, num_samples, int(from_snapshot),
+                                        out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out
+
+    def trace(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        self._ck(self.lib.pt_trace_rays(self.ctx, rays.ctypes.data_as(C.POINTER(capi.pt_ray)), rays.shape[0],
+                                        hits.ctypes.data_as(C.POINTER(capi.pt_hit))))
+        return hits
+
+    def shadow(self, rays: np.ndarray, maxd: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32)
+        maxd = np.ascontiguousarray(maxd, np.float32)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self._ck(self.lib.pt_trace_shadow(self.ctx, rays.ctypes.data_as(C.POINTER(capi.pt_ray)),
+                                          maxd.ctypes.data_as(C.POINTER(C.c_float)), rays.shape[0],
+                                          occ.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return occ
+
+    def stats(self) -> dict:
+        s = capi.pt_stats()
+        self._ck(self.lib.pt_get_stats(self.ctx, C.byref(s)))
+        return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
+                    status=s.status)
+
+    def update_instances(self, transforms, materials, tlas_nodes):
+        t = np.ascontiguousarray(transforms, np.float32)
+        m = np.ascontiguousarray(materials, np.float32)
+        n = np.ascontiguousarray(tlas_nodes, np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._ck(self.lib.pt_update_instances(self.ctx, fp(t), t.shape[0], fp(m), m.shape[0], fp(n), n.shape[0]))
+
+    def close(self):
+        if self.ctx:
+            self.lib.pt_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -204,10 +204,17 @@ int pt_render_passes(pt_context* ctx, int32_t first_pass, int32_t num_passes);
  * memory: render_width*render_height*4 floats. */
 int pt_get_accum(pt_context* ctx, float* host_rgba);
 
+/* Replaces: the buffer flip at the end of a sample pass
+ * (src/core/Renderer.cpp:756-760), after which GetOutputBuffer shows the
+ * completed pass: copies the accumulation buffer to the context's snapshot. */
+int pt_snapshot_accum(pt_context* ctx);
+
 /* Replaces: tonemap.glsl + Renderer::GetOutputBuffer (src/shaders/tonemap.glsl:97-133,
  * src/core/Renderer.cpp:619-634): accum / num_samples, tonemapped and gamma
- * corrected, written as RGBA8 into host memory (w*h*4 bytes, bottom row first). */
-int pt_get_output(pt_context* ctx, int32_t num_samples, uint8_t* host_rgba8);
+ * corrected, written as RGBA8 into host memory (w*h*4 bytes, bottom row first).
+ * from_snapshot = 1 reads the copy taken by pt_snapshot_accum instead of the
+ * live accumulation. */
+int pt_get_output(pt_context* ctx, int32_t num_samples, int32_t from_snapshot, uint8_t* host_rgba8);
 
 /* Test hook: closest-hit queries (closest_hit.glsl:25-266, triangle part)
  * over the device BVH for n host rays. */

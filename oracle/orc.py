@@ -32,7 +32,8 @@ def lib():
             build()
         _lib = C.CDLL(LIB)
         P = C.c_void_p
-        _lib.orc_render.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P]
+        _lib.orc_render.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, C.c_int]
+        _lib.orc_closest_hit_full.argtypes = [P, P, C.c_int, P, P, P, P, P]
         _lib.orc_trace_closest.argtypes = [P, P, C.c_int, P, C.c_int, C.c_int, P]
         _lib.orc_trace_any.argtypes = [P, P, P, P, C.c_int, P, C.c_int]
         _lib.orc_bsdf_eval.argtypes = [C.c_int, P, P, P, P, C.c_int, P, P, P, P]
@@ -47,18 +48,30 @@ def _p(a):
 
 
 def render(scene, options, camera, first_pass=0, num_passes=1, use_double=False, row_start=0, row_step=1,
-           nthreads=0, with_sq=False):
-    """Oracle render of sample passes; returns (accum[H,W,4], accum_sq or None, counters dict)."""
+           nthreads=0, with_sq=False, cull=False):
+    """Oracle render of sample passes; returns (accum[H,W,4], accum_sq or None, counters dict).
+    cull=True counts traversal work with tmax culling (the hits are the same)."""
     W, H = options.render_width, options.render_height
     accum = np.zeros((H, W, 4), np.float32)
     sq = np.zeros((H, W, 3), np.float32) if with_sq else None
     cnt = np.zeros(6, np.uint64)
     d = scene.desc()
     rc = lib().orc_render(C.byref(d), C.byref(options), C.byref(camera), first_pass, num_passes, int(use_double),
-                          row_start, row_step, nthreads, _p(accum), _p(sq), _p(cnt))
+                          row_start, row_step, nthreads, _p(accum), _p(sq), _p(cnt), int(cull))
     assert rc == 0
     keys = ["closest", "shadow", "nodes", "tris", "overflow", "paths"]
     return accum, sq, dict(zip(keys, [int(x) for x in cnt]))
+
+
+def closest_hit_full(scene, rays):
+    """Full ClosestHit (lights, triangles, shading normal) as the reference
+    build's ref_glsl_closest_hit reports it."""
+    n = rays.shape[0]
+    hit = np.zeros(n, np.int32); t = np.zeros(n, np.float32); mat = np.zeros(n, np.int32)
+    emi = np.zeros(n, np.int32); nrm = np.zeros((n, 3), np.float32)
+    d = scene.desc()
+    lib().orc_closest_hit_full(C.byref(d), _p(rays), n, _p(hit), _p(t), _p(mat), _p(emi), _p(nrm))
+    return dict(hit=hit, t=t, mat=mat, emitter=emi, normal=nrm)
 
 
 def rays_array(origins, dirs):

@@ -13,9 +13,10 @@ namespace {
 
 template <class R> int render_impl(const pt_scene_desc* d, const pt_render_options* o, const pt_camera* cam,
                                    int first_pass, int num_passes, int row_start, int row_step, int nthreads,
-                                   float* accum, float* accum_sq, uint64_t* counters) {
+                                   float* accum, float* accum_sq, uint64_t* counters, int cull) {
     Scene<R> s;
     MakeScene(s, d, o);
+    s.cull = cull != 0;
     const int W = o->render_width, H = o->render_height;
     if (row_step < 1) row_step = 1;
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -167,12 +168,14 @@ extern "C" {
 // RGB radiance + alpha) and accum_sq (W*H*3, sum of squares; may be NULL).
 // counters (6 x uint64): closest-hit queries, shadow queries, node visits,
 // triangle tests, stack overflows, paths.
+// cull = 1 counts node visits / triangle tests of a tmax-culled traversal
+// (same hits; the work counts define the roofline's bytes per ray).
 int orc_render(const pt_scene_desc* d, const pt_render_options* o, const pt_camera* cam, int first_pass,
                int num_passes, int use_double, int row_start, int row_step, int nthreads, float* accum,
-               float* accum_sq, uint64_t* counters) {
+               float* accum_sq, uint64_t* counters, int cull) {
     if (!d || !o || !cam || !accum) return 1;
-    return use_double ? render_impl<double>(d, o, cam, first_pass, num_passes, row_start, row_step, nthreads, accum, accum_sq, counters)
-                      : render_impl<float>(d, o, cam, first_pass, num_passes, row_start, row_step, nthreads, accum, accum_sq, counters);
+    return use_double ? render_impl<double>(d, o, cam, first_pass, num_passes, row_start, row_step, nthreads, accum, accum_sq, counters, cull)
+                      : render_impl<float>(d, o, cam, first_pass, num_passes, row_start, row_step, nthreads, accum, accum_sq, counters, cull);
 }
 
 // Closest triangle hit per ray over the flattened BVH.  mode 0: the
@@ -215,6 +218,33 @@ int orc_camera_rays(const pt_render_options* o, const pt_camera* cam, int pass, 
         rays[i].origin[0] = r.origin.x; rays[i].origin[1] = r.origin.y; rays[i].origin[2] = r.origin.z;
         rays[i].direction[0] = r.direction.x; rays[i].direction[1] = r.direction.y; rays[i].direction[2] = r.direction.z;
         if (rng_state) for (int k = 0; k < 4; ++k) rng_state[4 * i + k] = rng.s[k];
+    }
+    return 0;
+}
+
+// The full ClosestHit (lights + triangles + shading normal) on a ray set,
+// with State.depth = 1 so that emitters are intersected; the outputs match
+// ref_glsl_closest_hit of the reference build.
+int orc_closest_hit_full(const pt_scene_desc* d, const pt_ray* rays, int n, int* hit, float* t, int* matID,
+                         int* isEmitter, float* normal) {
+    pt_render_options o{};
+    o.max_depth = 1;
+    Scene<float> s;
+    MakeScene(s, d, &o);
+    for (int i = 0; i < n; ++i) {
+        Ray<float> r{V3<float>(rays[i].origin[0], rays[i].origin[1], rays[i].origin[2]),
+                     V3<float>(rays[i].direction[0], rays[i].direction[1], rays[i].direction[2])};
+        State<float> st;
+        st.depth = 1;
+        st.matID = -1;
+        LightSampleRec<float> ls;
+        Counters c;
+        bool h = ClosestHit(s, r, st, ls, c);
+        hit[i] = h ? 1 : 0;
+        t[i] = h ? st.hitDist : 1000000.0f;
+        matID[i] = h ? st.matID : -1;
+        isEmitter[i] = h && st.isEmitter ? 1 : 0;
+        normal[3 * i] = st.normal.x; normal[3 * i + 1] = st.normal.y; normal[3 * i + 2] = st.normal.z;
     }
     return 0;
 }

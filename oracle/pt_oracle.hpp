@@ -213,6 +213,7 @@ template <class R> struct Scene {
     R env_w, env_h, env_total, env_intensity, env_rot, mollify_amt;
     V3<R> uniform_light_col;
     bool has_textures;
+    bool cull = false;  // count work with tmax culling (mode 1) instead of the reference's traversal
 
     V3<R> node_min(int i) const { const float* p = d->bvh_nodes + 9 * (size_t)i; return {R(p[0]), R(p[1]), R(p[2])}; }
     V3<R> node_max(int i) const { const float* p = d->bvh_nodes + 9 * (size_t)i; return {R(p[3]), R(p[4]), R(p[5])}; }
@@ -522,7 +523,7 @@ template <class R> inline bool ClosestHit(const Scene<R>& s, const Ray<R>& r, St
     }
     TriHit<R> h;
     h.t = t;
-    TraverseClosest(s, r, t, h, &cnt, 0);
+    TraverseClosest(s, r, t, h, &cnt, s.cull ? 1 : 0);
     if (h.prim >= 0) t = h.t;
     if (t == K<R>::INF) return false;
 
@@ -627,8 +628,13 @@ template <class R> inline bool AnyHit(const Scene<R>& s, const Ray<R>& r, R maxD
             currMatID = rightIndex;
             continue;
         } else {
-            R leftHit = AABBIntersect(s.node_min(leftIndex), s.node_max(leftIndex), rTrans);
-            R rightHit = AABBIntersect(s.node_min(rightIndex), s.node_max(rightIndex), rTrans);
+            R l0, r0;
+            R leftHit = AABBIntersect(s.node_min(leftIndex), s.node_max(leftIndex), rTrans, &l0);
+            R rightHit = AABBIntersect(s.node_min(rightIndex), s.node_max(rightIndex), rTrans, &r0);
+            if (s.cull) {  // boxes entered beyond maxDist cannot occlude
+                if (leftHit > R(0) && l0 >= maxDist) leftHit = R(-1);
+                if (rightHit > R(0) && r0 >= maxDist) rightHit = R(-1);
+            }
             if (leftHit > R(0) && rightHit > R(0)) {
                 int deferred;
                 if (leftHit > rightHit) { index = rightIndex; deferred = leftIndex; }

@@ -1,0 +1,253 @@
+"""CUDA path (through the C ABI) against the oracle and the reference's
+golden fixtures.  Needs a GPU.
+
+Tolerances:
+  * ray queries: triangle id, instance id and the distance t are compared
+    exactly (the triangle test repeats the reference's float operations);
+    a different triangle is accepted only at the same distance (a tie,
+    |dt| <= 1e-6 t), or for a ray grazing a shared edge, where the oracle in
+    FP64 finds the CUDA triangle valid within 1e-6 in barycentrics; at most
+    1e-4 of the rays may fall in the second class.
+  * images: same seeds, so per-pixel agreement is expected up to the
+    last-ulp differences of CUDA's and the host's math libraries, which can
+    flip a discrete choice (Russian roulette, lobe selection) on a few
+    samples: >= 99% of pixels within 1e-3 relative (1e-4 absolute) and the
+    image means within 1e-3 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def world_points_on_tris(sd, n, rng):
+    """Random points on random triangles, in world space (instance transform)."""
+    nodes, top = sd.bvh_nodes, sd.top_level_index
+    leaves = [i for i in range(top, nodes.shape[0]) if nodes[i, 8] < 0]
+    pts = []
+    for _ in range(n):
+        li = leaves[rng.randint(len(leaves))]
+        inst, root = int(-nodes[li, 8] - 1), int(nodes[li, 6])
+        node = root
+        while nodes[node, 8] == 0:
+            node = int(nodes[node, 6] if rng.rand() < 0.5 else nodes[node, 7])
+        t = int(nodes[node, 6]) + rng.randint(int(nodes[node, 7]))
+        b = rng.dirichlet([1, 1, 1])
+        P = sum(b[k] * sd.vertices_uvx[sd.vert_indices[t, k], :3].astype(np.float64) for k in range(3))
+        M = sd.transforms[inst].reshape(4, 4).astype(np.float64)
+        pts.append((np.r_[P, 1.0] @ M)[:3])
+    return np.array(pts)
+
+
+def ray_set(sd, orc, n, seed):
+    rng = np.random.RandomState(seed)
+    o = sd.render_options()
+    W, H = o.render_width, o.render_height
+    px = rng.randint(0, W, n // 2)
+    py = rng.randint(0, H, n // 2)
+    cam_rays, _ = orc.camera_rays(o, sd.pt_camera(), 0, px, py)
+    P = world_points_on_tris(sd, n - n // 2, rng)
+    d = rng.normal(size=P.shape)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    sec = orc.rays_array((P + d * 3e-4).astype(np.float32), d.astype(np.float32))
+    return np.ascontiguousarray(np.concatenate([cam_rays, sec]), np.float32)
+
+
+def scene_by_name(name):
+    from pathtracer import scenes
+    if name == "ref_cornell":
+        return golden_scene("ref_scene_cornell_box_orig.npz")
+    if name == "ref_volume":
+        return golden_scene("ref_scene_volume_cube.npz")
+    if name == "cornell":
+        return scenes.cornell(64, 64, tile=32)
+    if name == "icosphere":
+        return scenes.icosphere_scene(freq=60, width=96, height=64, tile=32)
+    if name == "instanced":
+        return scenes.instanced_scene(num_instances=300, tris_per_blas=3000, width=96, height=64,
+                                      env_size=(256, 128), tile=32)
+    raise KeyError(name)
+
+
+SCENES = ["ref_cornell", "ref_volume", "cornell", "icosphere", "instanced"]
+
+
+def classify_mismatch(sd, orc, rays, h_gpu, h_orc):
+    """Indices where the hits differ beyond a tie."""
+    diff = (h_gpu["prim_id"] != h_orc["prim_id"]) | (h_gpu["inst_id"] != h_orc["inst_id"])
+    tie = diff & (h_gpu["prim_id"] >= 0) & (h_orc["prim_id"] >= 0) & (
+        np.abs(h_gpu["t"] - h_orc["t"]) <= 1e-6 * np.abs(h_orc["t"]))
+    return np.where(diff & ~tie)[0], int(tie.sum())
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_closest_hit_parity(ptlib, orc, name):
+    from pathtracer.renderer import GpuRenderer
+    sd = scene_by_name(name)
+    rays = ray_set(sd, orc, 20000, 1)
+    with GpuRenderer(sd) as r:
+        hg = r.trace(rays)
+    ho, cnt = orc.trace_closest(sd, rays, mode=0)
+    assert cnt["overflow"] == 0
+    bad, ties = classify_mismatch(sd, orc, rays, hg, ho)
+    assert len(bad) <= max(2, int(1e-4 * len(rays))), (name, len(bad), ties, hg[bad[:5]], ho[bad[:5]])
+    same = (hg["prim_id"] == ho["prim_id"]) & (hg["inst_id"] == ho["inst_id"])
+    # identical triangle => identical float distance and barycentrics
+    assert np.array_equal(hg["t"][same], ho["t"][same])
+    assert np.array_equal(hg["u"][same], ho["u"][same])
+    assert np.array_equal(hg["v"][same], ho["v"][same])
+    assert (hg["prim_id"] >= 0).mean() > 0.3
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_any_hit_parity(ptlib, orc, name):
+    from pathtracer.renderer import GpuRenderer
+    sd = scene_by_name(name)
+    rays = ray_set(sd, orc, 20000, 2)
+    rng = np.random.RandomState(3)
+    ho, _ = orc.trace_closest(sd, rays, mode=0)
+    # max distances around the closest hit: just before, just after, far
+    maxd = np.where(ho["prim_id"] >= 0, ho["t"] * rng.choice([0.5, 0.999, 1.001, 2.0], len(rays)), 1e5).astype(np.float32)
+    o = sd.render_options()
+    with GpuRenderer(sd) as r:
+        og = r.shadow(rays, maxd)
+    oo = orc.trace_any(sd, o, rays, maxd)
+    diff = np.where(og != oo)[0]
+    assert len(diff) <= max(2, int(1e-4 * len(rays))), (name, len(diff))
+
+
+def image_agreement(a, b):
+    rel = np.abs(a[..., :3] - b[..., :3]) / np.maximum(np.abs(b[..., :3]), 1e-1)
+    ok = np.all((rel < 1e-3) | (np.abs(a[..., :3] - b[..., :3]) < 1e-4), axis=-1)
+    mean_rel = abs(a[..., :3].mean() - b[..., :3].mean()) / max(b[..., :3].mean(), 1e-6)
+    return ok.mean(), mean_rel
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_render_matches_oracle(ptlib, orc, name):
+    from pathtracer.renderer import GpuRenderer
+    sd = scene_by_name(name)
+    o = sd.render_options()
+    passes = 4
+    with GpuRenderer(sd) as r:
+        r.render_passes(0, passes)
+        acc = r.accum()
+        st = r.stats()
+    ref, _, cnt = orc.render(sd, o, sd.pt_camera(), 0, passes)
+    frac, mean_rel = image_agreement(acc, ref)
+    assert st["status"] == 0
+    assert st["paths"] == o.render_width * o.render_height * passes
+    assert frac >= 0.99, (name, frac)
+    assert mean_rel < 1e-3, (name, mean_rel)
+    assert np.array_equal(acc[..., 3], ref[..., 3])
+    total_gpu = st["closest"] + st["shadow"]
+    total_orc = cnt["closest"] + cnt["shadow"]
+    assert abs(total_gpu - total_orc) <= 0.01 * total_orc
+
+
+@pytest.mark.parametrize("name,scene_file", [
+    ("cornell_box_orig", "ref_scene_cornell_box_orig.npz"),
+    ("volume_cube", "ref_scene_volume_cube.npz"),
+    ("cornell_c1_48", "scene_cornell_c1_48.npz"),
+])
+def test_render_matches_reference_shaders(ptlib, name, scene_file):
+    """Against the accumulation of the reference's own shader source."""
+    from pathtracer.renderer import GpuRenderer
+    sd = golden_scene(scene_file)
+    g = golden(f"ref_render_{name}.npz")
+    o = sd.render_options(render_width=int(g["width"]), render_height=int(g["height"]),
+                          tile_width=int(g["tile_w"]), tile_height=int(g["tile_h"]))
+    with GpuRenderer(sd, o) as r:
+        r.render_passes(0, int(g["passes"]))
+        acc = r.accum()
+    frac, mean_rel = image_agreement(acc, g["accum"])
+    assert frac >= 0.99 and mean_rel < 1e-3, (name, frac, mean_rel)
+
+
+def test_tiles_equal_whole_passes(ptlib):
+    """pt_render_tile in the reference's tile order (Renderer.cpp:745-762)
+    gives the same accumulation, bit for bit, as pt_render_passes."""
+    from pathtracer import scenes
+    from pathtracer.renderer import GpuRenderer
+    sd = scenes.cornell(80, 48, tile=32)  # ragged last tile column/row
+    o = sd.render_options()
+    ntx, nty = (80 + 31) // 32, (48 + 31) // 32
+    with GpuRenderer(sd) as r:
+        r.render_passes(0, 2)
+        a = r.accum()
+        r.clear()
+        frame = 2
+        for _ in range(2):
+            for ty in range(nty - 1, -1, -1):
+                for tx in range(ntx):
+                    r.render_tile(tx, ty, frame)
+                    frame += 1
+        b = r.accum()
+    assert np.array_equal(a, b)
+
+
+def test_tonemap_output(ptlib, orc):
+    """pt_get_output against tonemap.glsl restated in numpy (Reinhard on
+    luminance with limit 1.5, gamma 1/2.2, RGBA8 round-half-up)."""
+    from pathtracer import scenes
+    from pathtracer.renderer import GpuRenderer
+    sd = scenes.cornell(64, 64)
+    with GpuRenderer(sd) as r:
+        r.render_passes(0, 3)
+        acc = r.accum()
+        ldr = r.output(3)
+        r.snapshot()
+        r.render_passes(3, 1)
+        snap = r.output(3, from_snapshot=True)
+    c = acc[..., :3].astype(np.float32) * np.float32(1.0 / 3.0)
+    lum = (np.float32(0.212671) * c[..., 0] + np.float32(0.715160) * c[..., 1]) + np.float32(0.072169) * c[..., 2]
+    c = c / (np.float32(1.0) + lum / np.float32(1.5))[..., None]
+    c = np.power(np.maximum(c, 0), np.float32(1.0 / 2.2))
+    exp = np.floor(np.clip(c, 0, 1) * 255 + 0.5).astype(np.int32)
+    assert np.abs(ldr[..., :3].astype(np.int32) - exp).max() <= 1
+    assert np.all(ldr[..., 3] == 255)
+    assert np.array_equal(snap, ldr)
+
+
+def test_z_test_converged(ptlib, orc):
+    """Independent sample sets (oracle passes 0-63, CUDA passes 64-127) agree
+    within the Monte Carlo noise: per-pixel z-scores."""
+    from pathtracer import scenes
+    from pathtracer.renderer import GpuRenderer
+    sd = scenes.cornell(32, 32, tile=32)
+    o = sd.render_options()
+    n = 64
+    ref, sq, _ = orc.render(sd, o, sd.pt_camera(), 0, n, with_sq=True)
+    with GpuRenderer(sd) as r:
+        r.render_passes(n, n)
+        acc = r.accum()
+    mu_r = ref[..., :3] / n
+    var = np.maximum(sq / n - mu_r ** 2, 1e-12)
+    z = (acc[..., :3] / n - mu_r) / np.sqrt(2 * var / n)
+    assert abs(z.mean()) < 0.1
+    assert (np.abs(z) > 4).mean() < 2e-3
+
+
+def test_error_paths(ptlib):
+    """Bad arguments come back as PT_ERR_* codes with a message."""
+    import ctypes as C
+    from pathtracer import capi, scenes
+    from pathtracer.renderer import GpuRenderer
+    lib = ptlib
+    sd = scenes.cornell(16, 16)
+    with GpuRenderer(sd) as r:
+        assert lib.pt_render_tile(r.ctx, 99, 0, 2) == capi.PT_ERR_INVALID_ARG
+        assert lib.pt_render_passes(r.ctx, -1, 1) == capi.PT_ERR_INVALID_ARG
+        assert lib.pt_set_integrator(r.ctx, 7) == capi.PT_ERR_INVALID_ARG
+    bad = scenes.cornell(16, 16)
+    bad.materials[1, 24] = 0.0  # a texture map id: not supported yet
+    with pytest.raises(capi.PTError) as e:
+        GpuRenderer(bad)
+    assert e.value.code == capi.PT_ERR_UNSUPPORTED
+    bad2 = scenes.cornell(16, 16)
+    bad2.bvh_nodes[bad2.top_level_index, 6] = 10 ** 6  # child index out of range
+    with pytest.raises(capi.PTError) as e:
+        GpuRenderer(bad2)
+    assert e.value.code == capi.PT_ERR_INVALID_ARG
