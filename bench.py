@@ -1,0 +1,339 @@
+"""Throughput benchmark of the GB300 path tracer.
+
+Default workload: the 1M-triangle scene (geodesic icosphere, 1,048,820
+triangles, 3-octave value-noise displacement, 16 Disney materials, one sphere
+light), 1920x1080, 16 spp, max depth 8, FP32.  One step = one 16-spp frame
+(16 sample passes in one launch).  Metric: Mrays/s, rays = executed
+closest-hit queries + shadow queries (any-hit calls and transmittance
+segments), counted on the device.
+
+  value      device-resident: per-step CUDA events on the launching stream
+             around the render launch; the L2 is flushed (a 512 MiB write)
+             before every timed step.
+  e2e        through the public C ABI with host buffers, wall clock per step:
+             pt_set_camera + pt_render_passes + pt_get_output (tonemapped
+             RGBA8 image copied to pinned host memory).
+  roofline   HBM: algorithmic bytes per ray (36 B per node visit + 60 B per
+             triangle test + 176 B per triangle hit, counted by the oracle with
+             a tmax-culled traversal of the reference's binary BVH on a row
+             sample) x rays per launch / kernel time, against MEASURED_PEAKS.json.
+  cpu_baseline  the oracle (C++ restatement of the reference's shaders, the
+             reference's traversal, FP32, OpenMP on all host cores) on a row
+             sample of the same frame.
+
+--impl reference times the CPU restatement of the reference (the reference's
+GLSL cannot run without a graphics stack; its own source builds only where
+the reference is present, not on the GPU machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "glsl-pathtracer_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mrays/s @1080p depth8 1M tris"
+CONFIGS = {
+    "icosphere_1m": dict(desc="icosphere 1,048,820 tris, 1920x1080, 16 spp, depth 8", freq=229, width=1920,
+                         height=1080, spp=16, depth=8),
+    "cornell": dict(desc="procedural Cornell box 256x256, 64 spp, depth 4", width=256, height=256, spp=64, depth=4),
+    "instanced": dict(desc="10,000 instances of 5 x 50k-tri BLAS + IBL + volume, 1920x1080, 16 spp, depth 8",
+                      width=1920, height=1080, spp=16, depth=8),
+}
+
+
+def make_scene(name, cfg, small=False):
+    from pathtracer import scenes
+    if name == "icosphere_1m":
+        return scenes.icosphere_scene(freq=cfg["freq"] if not small else 40, width=cfg["width"], height=cfg["height"],
+                                      max_depth=cfg["depth"])
+    if name == "cornell":
+        return scenes.cornell(cfg["width"], cfg["height"], max_depth=cfg["depth"])
+    if name == "instanced":
+        return scenes.instanced_scene(width=cfg["width"], height=cfg["height"], max_depth=cfg["depth"])
+    raise KeyError(name)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
+    """Oracle work counts (tmax-culled traversal of the reference's binary
+    BVH) on a row sample -> algorithmic bytes per ray query."""
+    import orc
+    _, _, c = orc.render(scene, options, camera, 0, passes, row_step=row_step, cull=True)
+    rays = c["closest"] + c["shadow"]
+    b = (36.0 * c["nodes"] + 60.0 * c["tris"] + 176.0 * c["tri_hits"]) / max(rays, 1)
+    return b, dict(nodes_per_ray=c["nodes"] / rays, tris_per_ray=c["tris"] / rays,
+                   hits_per_ray=c["tri_hits"] / rays, rays=rays)
+
+
+def cpu_baseline(scene, options, camera, spp, target_s=15.0):
+    """The oracle on a row sample of the frame, all host threads."""
+    import orc
+    H = options.render_height
+    ncores = os.cpu_count() or 1
+    # calibrate on a thin sample, then size the sample for ~target_s seconds
+    step = max(1, H // 8)
+    t0 = time.perf_counter()
+    _, _, c = orc.render(scene, options, camera, 0, spp, row_step=step)
+    dt = time.perf_counter() - t0
+    rows = max(1, len(range(0, H, step)))
+    per_row = dt / rows
+    want_rows = max(1, min(H, int(target_s / max(per_row, 1e-6))))
+    step = max(1, H // want_rows)
+    t0 = time.perf_counter()
+    _, _, c = orc.render(scene, options, camera, 0, spp, row_step=step)
+    dt = time.perf_counter() - t0
+    rays = c["closest"] + c["shadow"]
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": ncores, "kind": "port",
+            "sample": f"every {step}th row of the {options.render_width}x{H} frame, {spp} spp, depth "
+                      f"{options.max_depth} ({rays} rays in {dt:.1f} s; oracle FP32, OpenMP)"}, rays, dt
+
+
+def run_reference(args, cfg, name):
+    """--impl reference: the reference's algorithm restated on the CPU, timed
+    on bounded row samples of the same frame; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sd = make_scene(name, cfg)
+    o = sd.render_options()
+    cam = sd.pt_camera()
+    import orc
+    H = o.render_height
+    step = max(1, H // 16)
+    for _ in range(args.warmup):
+        orc.render(sd, o, cam, 0, 1, row_step=H)  # one row
+    tot_rays, tot_t = 0, 0.0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, c = orc.render(sd, o, cam, 0, cfg["spp"], row_start=k % step, row_step=step)
+        tot_t += time.perf_counter() - t0
+        tot_rays += c["closest"] + c["shadow"]
+    v = tot_rays / tot_t / 1e6
+    ncores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["desc"] + f"; each step renders every {step}th row"},
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": ncores, "kind": "port",
+                         "sample": f"every {step}th row per step, {cfg['spp']} spp; the reference's shaders restated "
+                                   "in C++ (its GLSL needs OpenGL, unavailable on this machine)"},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="icosphere_1m", choices=sorted(CONFIGS))
+    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
+    ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
+    args = ap.parse_args()
+    cfg = dict(CONFIGS[args.config])
+    if args.spp:
+        cfg["spp"] = args.spp
+        cfg["desc"] += f" [profiling run: {args.spp} spp per step]"
+    if args.impl == "reference":
+        return run_reference(args, cfg, args.config)
+
+    import torch
+    from pathtracer import build, capi
+    from pathtracer.renderer import GpuRenderer
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build_library()
+    sd = make_scene(args.config, cfg, small=args.small)
+    spp = cfg["spp"]
+    r = GpuRenderer(sd)
+    r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else capi.PT_INTEGRATOR_MEGAKERNEL)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    # each rank renders its own range of sample passes of the same frame
+    pass_base = rank * spp * (args.steps + args.warmup + 8)
+
+    def step(k):
+        r.render_passes(pass_base + k * spp, spp)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            step(k)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    rays = 0
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)  # L2 flush between timed steps
+                starts[k].record(stream)
+                step(args.warmup + k)
+                ends[k].record(stream)
+            st = r.stats()  # synchronises; counters of this launch
+            rays += st["closest"] + st["shadow"]
+            if st["status"] != 0:
+                raise RuntimeError(f"kernel status {st['status']}")
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_total = sum(ms) / 1000.0
+    if dist:
+        t = torch.tensor([t_total, float(rays)], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        t_total, rays = float(tmax[0]), int(t[1])
+    value = rays / t_total / 1e6
+    rays_per_step = rays / (args.steps * world)
+
+    # end to end through the C ABI with host buffers
+    import ctypes as C
+    lib = capi.load_library()
+    r.set_stream(None)
+    out = torch.empty((r.height, r.width, 4), dtype=torch.uint8).pin_memory()
+    cam = sd.pt_camera()
+    e2e_rays = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        capi.check(lib, lib.pt_set_camera(r.ctx, C.byref(cam)))
+        capi.check(lib, lib.pt_render_passes(r.ctx, pass_base + (args.warmup + args.steps + k) * spp, spp))
+        capi.check(lib, lib.pt_get_output(r.ctx, spp, 0, C.cast(out.data_ptr(), C.POINTER(C.c_uint8))))
+        st = r.stats()
+        e2e_rays += st["closest"] + st["shadow"]
+    e2e_t = time.perf_counter() - t0
+    e2e = {"value": e2e_rays / e2e_t / 1e6 * world, "unit": "Mrays/s",
+           "h2d_bytes_per_step": C.sizeof(capi.pt_camera),
+           "d2h_bytes_per_step": int(r.width * r.height * 4)}
+
+    line = None
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        b_ray, work = bytes_per_ray(sd, sd.render_options(), cam)
+        mean_ms = statistics.mean(ms)
+        achieved = b_ray * rays_per_step / (mean_ms / 1000.0) / 1e9
+        traffic = None
+        tfile = os.path.join(ROOT, "profiles", "traffic_per_ray.json")
+        if os.path.exists(tfile):
+            with open(tfile) as fh:
+                tp = json.load(fh)
+            if tp.get("config") == args.config and tp.get("integrator") == args.integrator:
+                traffic = tp["dram_bytes_per_ray"] * rays_per_step
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu, _, _ = cpu_baseline(sd, sd.render_options(), cam, spp)
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["desc"] + ("" if not args.small else " (small variant)"),
+                       "integrator": args.integrator, "rays_per_step": rays_per_step,
+                       "l2": "flushed before each timed step (512 MiB write)",
+                       "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU"},
+            "gpu_launches": args.steps * world,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "bytes_per_ray": b_ray, **work},
+            "e2e": e2e,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

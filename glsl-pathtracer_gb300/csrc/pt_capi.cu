@@ -9,10 +9,13 @@
 #include <string>
 #include <vector>
 
+#include <cstdlib>
+
 #include "../../include/pt_cuda.h"
 #include "bvh8.h"
 #include "pt_device.cuh"
 #include "pt_params.h"
+#include "pt_wavefront.h"
 
 using namespace ptgb;
 
@@ -92,6 +95,9 @@ struct pt_context {
     DevBuf<unsigned long long> counters;
     DevBuf<int> status;
     pt_stats last{};
+    WavefrontBuffers wf;
+    WavefrontTuning wf_tuning;
+    bool wf_tuned = false;
 };
 
 namespace {
@@ -247,6 +253,35 @@ int end_launch(pt_context* c) {
     return PT_OK;
 }
 
+// Paths per wavefront batch: PT_WAVEFRONT_CAPACITY (default 2^24, about
+// 4.8 GB of path state), at least one full pass of the frame.
+int wavefront_capacity(const pt_context* c, const RenderWork& w) {
+    long cap = 1L << 24;
+    if (const char* s = std::getenv("PT_WAVEFRONT_CAPACITY")) cap = std::max(1L, std::atol(s));
+    const long npix = (long)w.w * w.h;
+    const long want = std::min((long)w.num_passes * npix, std::max(cap, npix));
+    return (int)std::min(want, (long)INT32_MAX / 2);
+}
+
+int render(pt_context* c, const RenderWork& w) {
+    if (int rc = begin_launch(c)) return rc;
+    const Params p = make_params(c);
+    if (c->integrator == PT_INTEGRATOR_WAVEFRONT) {
+        const int cap = wavefront_capacity(c, w);
+        if (c->wf.capacity < cap) CK(wavefront_alloc(c->wf, cap));
+        if (!c->wf_tuned) {
+            CK(wavefront_default_tuning(c->wf_tuning, 128));
+            c->wf_tuned = true;
+        }
+        const char* g = std::getenv("PT_WAVEFRONT_GRAPH");
+        const bool use_graph = !(g && g[0] == '0');
+        CK(launch_wavefront(p, w, c->wf, c->wf_tuning, use_graph, c->stream));
+    } else {
+        CK(launch_render(p, w, c->integrator, c->stream));
+    }
+    return end_launch(c);
+}
+
 }  // namespace
 
 extern "C" {
@@ -346,6 +381,7 @@ int pt_destroy(pt_context* c) {
     c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->vidx.free(); c->verts.free();
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
     c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();
+    wavefront_free(c->wf);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -446,9 +482,7 @@ int pt_render_tile(pt_context* c, int32_t tx, int32_t ty, int32_t frame) {
     w.tile_frame = frame;
     w.tile_x = tx;
     w.tile_y = ty;
-    if (int rc = begin_launch(c)) return rc;
-    CK(launch_render(make_params(c), w, c->integrator, c->stream));
-    return end_launch(c);
+    return render(c, w);
 }
 
 int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {
@@ -462,9 +496,7 @@ int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {
     w.num_passes = num_passes;
     w.tile_frame = -1;
     w.tile_x = w.tile_y = 0;
-    if (int rc = begin_launch(c)) return rc;
-    CK(launch_render(make_params(c), w, c->integrator, c->stream));
-    return end_launch(c);
+    return render(c, w);
 }
 
 int pt_get_accum(pt_context* c, float* host) {

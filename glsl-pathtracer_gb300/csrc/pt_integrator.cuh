@@ -1,0 +1,627 @@
+// pt_integrator.cuh - the path integrator of common/pathtrace.glsl as one
+// step per path vertex, shared by the megakernel and the wavefront kernels.
+//
+//   TraceClosest   ClosestHit's queries (closest_hit.glsl:25-218): analytic
+//                  lights, then the BVH; fills a HitRecord
+//   ShadeStep      one iteration of PathTrace's loop (pathtrace.glsl:301-473)
+//                  given the HitRecord: misses, emission, MIS, media, alpha
+//                  pass-through, next-event estimation (DirectLight,
+//                  pathtrace.glsl:158-283), BSDF sampling, Russian roulette
+//
+// Next-event estimation's shadow rays are traced inline (megakernel, and any
+// scene where the reference's AnyHit or EvalTransmittance consume random
+// numbers: alpha-tested materials, volumes with VOL_MIS) or returned as a
+// ShadowReq for a separate shadow stage (wavefront).  The contributions are
+// computed with the same operations either way, so both forms add the same
+// float values in the same order: a path renders identically in both.
+#pragma once
+
+#include "pt_trace.cuh"
+
+namespace ptgb {
+
+struct PathState {
+    Ray r;
+    V3 throughput, radiance;
+    float alpha;
+    Rng rng;
+    int depth;
+    int matID;          // state.matID: kept when the hit is a light (pathtrace.glsl:341)
+    float prevRough;    // state.mat.roughness of the last vertex (roughness mollification)
+    float scatterPdf;   // scatterSample.pdf of the last bounce (MIS weights)
+    bool inMedium, surfaceScatter;
+    Medium medium;      // state.medium
+};
+
+struct HitRecord {
+    bool hit, isEmitter;
+    float t, u, v, w;
+    int prim, inst, mat;
+    float lightPdf;
+    V3 lightEmission;
+};
+
+struct ShadowReq {
+    int n;              // shadow rays: bit 0 env ray, bit 1 light ray
+    int adds;           // bit k: ray k contributes when unoccluded
+    V3 origin;          // scatterPos (pathtrace.glsl:162)
+    V3 dir[2];
+    float maxd[2];
+    V3 contrib[2];      // misWeight * Li * f / pdf of ray k (env, light)
+    V3 T;               // throughput the result is multiplied by
+};
+
+struct Counters {
+    uint32_t closest, shadow;
+};
+
+// ------------------------------------------------------------ ClosestHit
+__device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int depth, HitRecord& hr, uint2* stack,
+                                             Counters& cnt, bool count_as_shadow) {
+    if (count_as_shadow) cnt.shadow++;
+    else cnt.closest++;
+    float t = PT_INF;
+    hr.isEmitter = false;
+    if ((P.flags & F_LIGHTS) && !((P.flags & F_HIDE_EMITTERS) && !(depth > 0))) {  // closest_hit.glsl:30-86
+        for (int i = 0; i < P.num_lights; i++) {
+            const Light L = LoadLight(P.lights, i);
+            const int type = (int)L.type;
+            if (type == QUAD_LIGHT) {
+                V3 normal = normalize(cross(L.u, L.v));
+                if (dot(normal, r.direction) > 0.0f) continue;
+                float pw = dot(normal, L.position);
+                V3 u = L.u * (1.0f / dot(L.u, L.u));
+                V3 v = L.v * (1.0f / dot(L.v, L.v));
+                float d = RectIntersect(L.position, u, v, normal, pw, r);
+                if (d < 0.0f) d = PT_INF;
+                if (d < t) {
+                    t = d;
+                    float cosTheta = dot(-r.direction, normal);
+                    hr.lightPdf = (t * t) / (L.area * cosTheta);
+                    hr.lightEmission = L.emission;
+                    hr.isEmitter = true;
+                }
+            }
+            if (type == SPHERE_LIGHT) {
+                float d = SphereIntersect(L.radius, L.position, r);
+                if (d < 0.0f) d = PT_INF;
+                if (d < t) {
+                    t = d;
+                    V3 hitPt = r.origin + t * r.direction;
+                    float cosTheta = dot(-r.direction, normalize(hitPt - L.position));
+                    hr.lightPdf = (t * t) / (L.area * cosTheta * 0.5f);
+                    hr.lightEmission = L.emission;
+                    hr.isEmitter = true;
+                }
+            }
+        }
+    }
+    TriHit h;
+    h.t = t;
+    h.prim = -1;
+    h.inst = -1;
+    h.mat = 0;
+    h.u = h.v = h.w = 0.0f;
+    traverse_closest<true>(P, P.tlas_root, prep_ray(r.origin, r.direction), h, stack, 0, -1, 0);
+    if (h.prim >= 0) {
+        t = h.t;
+        hr.isEmitter = false;
+    }
+    hr.hit = t != PT_INF;
+    hr.t = t;
+    hr.prim = h.prim;
+    hr.inst = h.inst;
+    hr.mat = h.mat;
+    hr.u = h.u;
+    hr.v = h.v;
+    hr.w = h.w;
+}
+
+// Shading attributes of a triangle hit (closest_hit.glsl:224-247).
+__device__ __forceinline__ void HitNormal(const Params& P, const HitRecord& hr, const Ray& r, V3& normal, V3& ffnormal) {
+    const int i0 = __ldg(P.vidx + 3 * hr.prim), i1 = __ldg(P.vidx + 3 * hr.prim + 1), i2 = __ldg(P.vidx + 3 * hr.prim + 2);
+    const V3 n0 = v3(__ldg(P.norms + i0)), n1 = v3(__ldg(P.norms + i1)), n2 = v3(__ldg(P.norms + i2));
+    V3 n = normalize(n0 * hr.w + n1 * hr.u + n2 * hr.v);  // bary = uvt.wxy
+    if (hr.inst >= 0) {
+        const float4* x = P.xf + 10 * hr.inst + 7;
+        const float4 c0 = __ldg(x), c1 = __ldg(x + 1), c2 = __ldg(x + 2);
+        n = v3(c0.x * n.x + c1.x * n.y + c2.x * n.z, c0.y * n.x + c1.y * n.y + c2.y * n.z,
+               c0.z * n.x + c1.z * n.y + c2.z * n.z);
+    }
+    normal = normalize(n);
+    ffnormal = dot(normal, r.direction) <= 0.0f ? normal : -normal;
+}
+
+// GetMaterial (pathtrace.glsl:25-115) without texture maps.
+__device__ __forceinline__ void GetMaterial(const Params& P, int matID, int depth, float prevRough, V3 normal,
+                                            const Ray& r, Material& mat, float& eta) {
+    LoadMaterial(P.mats, matID, mat);
+    if ((P.flags & F_MOLLIFY) && depth > 0) mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
+    FinishMaterial(mat);
+    eta = dot(r.direction, normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
+}
+
+__device__ __forceinline__ bool AlphaSkip(const Material& m, Rng& rng) {
+    if (m.alphaMode == ALPHA_MODE_MASK && m.opacity < m.alphaCutoff) return true;
+    if (m.alphaMode == ALPHA_MODE_BLEND) return rng.next() > m.opacity;
+    return false;
+}
+
+// anyhit.glsl:25-216
+__device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack, Counters& cnt) {
+    cnt.shadow++;
+    if (P.flags & F_LIGHTS) {
+        for (int i = 0; i < P.num_lights; i++) {
+            const Light L = LoadLight(P.lights, i);
+            const int type = (int)L.type;
+            if (type == QUAD_LIGHT) {
+                V3 normal = normalize(cross(L.u, L.v));
+                float pw = dot(normal, L.position);
+                V3 u = L.u * (1.0f / dot(L.u, L.u));
+                V3 v = L.v * (1.0f / dot(L.v, L.v));
+                float d = RectIntersect(L.position, u, v, normal, pw, r);
+                if (d > 0.0f && d < maxDist) return true;
+            }
+            if (type == SPHERE_LIGHT) {
+                float d = SphereIntersect(L.radius, L.position, r);
+                if (d > 0.0f && d < maxDist) return true;
+            }
+        }
+    }
+    const bool alpha = (P.flags & F_ALPHA_TEST) && !(P.flags & F_MEDIUM);
+    return traverse_any<true>(P, P.tlas_root, prep_ray(r.origin, r.direction), maxDist, stack, 0, 0, alpha, rng);
+}
+
+// pathtrace.glsl:118-156 (OPT_MEDIUM && OPT_VOL_MIS); each segment is counted
+// as a shadow query.
+__device__ __noinline__ V3 EvalTransmittance(const Params& P, Ray r, Rng& rng, uint2* stack, Counters& cnt) {
+    V3 transmittance = v3(1.0f);
+    int matID = 0;
+    for (int depth = 0; depth < P.max_depth; depth++) {
+        HitRecord hr;
+        TraceClosest(P, r, 0, hr, stack, cnt, true);
+        if (!hr.hit || hr.isEmitter) break;
+        V3 normal, ffnormal;
+        HitNormal(P, hr, r, normal, ffnormal);
+        matID = hr.mat;
+        Material mat;
+        float eta;
+        GetMaterial(P, matID, 0, 0.0f, normal, r, mat, eta);
+        bool alphatest = AlphaSkip(mat, rng);
+        bool refractive = (1.0f - mat.metallic) * mat.specTrans > 0.0f;
+        if (!(alphatest || refractive)) return v3(0.0f);
+        if (dot(r.direction, normal) > 0.0f && mat.medium.type != MEDIUM_NONE) {
+            V3 color = mat.medium.type == MEDIUM_ABSORB ? v3(1.0f) - mat.medium.color : v3(1.0f);
+            transmittance = transmittance * vexp(-color * mat.medium.density * hr.t);
+        }
+        r.origin = (r.origin + r.direction * hr.t) + r.direction * PT_EPS;
+    }
+    return transmittance;
+}
+
+// ------------------------------------------------------------ envmap
+// envmap.glsl:28-55
+__device__ __forceinline__ void BinarySearch(const Params& P, float value, float& u, float& v) {
+    const int W = P.env_w, H = P.env_h;
+    int lower = 0, upper = H - 1;
+    while (lower < upper) {
+        int mid = (lower + upper) >> 1;
+        if (value < __ldg(P.cdf + (size_t)mid * W + (W - 1))) upper = mid;
+        else lower = mid + 1;
+    }
+    const int y = min(max(lower, 0), H - 1);
+    lower = 0;
+    upper = W - 1;
+    while (lower < upper) {
+        int mid = (lower + upper) >> 1;
+        if (value < __ldg(P.cdf + (size_t)y * W + mid)) upper = mid;
+        else lower = mid + 1;
+    }
+    const int x = min(max(lower, 0), W - 1);
+    u = (float)x / (float)W;
+    v = (float)y / (float)H;
+}
+
+// texture(envMapTex, uv): bilinear, GL_REPEAT (Renderer.cpp:213-218)
+__device__ __forceinline__ V3 SampleEnv(const Params& P, float u, float v) {
+    const int W = P.env_w, H = P.env_h;
+    float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    float fx = floorf(x), fy = floorf(y);
+    float ax = x - fx, ay = y - fy;
+    int ix = (int)fx, iy = (int)fy;
+    int x0 = ix % W; x0 += x0 < 0 ? W : 0;
+    int y0 = iy % H; y0 += y0 < 0 ? H : 0;
+    int x1 = x0 + 1 == W ? 0 : x0 + 1;
+    int y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float4 a = __ldg(P.env + (size_t)y0 * W + x0), b = __ldg(P.env + (size_t)y0 * W + x1);
+    const float4 c = __ldg(P.env + (size_t)y1 * W + x0), d = __ldg(P.env + (size_t)y1 * W + x1);
+    V3 t0 = v3(a) * (1.0f - ax) + v3(b) * ax;
+    V3 t1 = v3(c) * (1.0f - ax) + v3(d) * ax;
+    return t0 * (1.0f - ay) + t1 * ay;
+}
+
+// envmap.glsl:57-66
+__device__ __forceinline__ V3 EvalEnvMap(const Params& P, const Ray& r, float& pdfOut) {
+    float theta = acosf(clampf(r.direction.y, -1.0f, 1.0f));
+    float u = (PT_PI + atan2f(r.direction.z, r.direction.x)) * PT_INV_TWO_PI + P.env_rot;
+    float v = theta * PT_INV_PI;
+    V3 color = SampleEnv(P, u, v);
+    float pdf = Luminance(color) / P.env_total;
+    pdfOut = (pdf * (float)P.env_w * (float)P.env_h) / (PT_TWO_PI * PT_PI * sinf(theta));
+    return color;
+}
+
+// envmap.glsl:68-83
+__device__ __forceinline__ V3 SampleEnvMap(const Params& P, V3& color, float& pdfOut, Rng& rng) {
+    float u, v;
+    BinarySearch(P, rng.next() * P.env_total, u, v);
+    color = SampleEnv(P, u, v);
+    float pdf = Luminance(color) / P.env_total;
+    u -= P.env_rot;
+    float phi = u * PT_TWO_PI;
+    float theta = v * PT_PI;
+    float st = sinf(theta), ct = cosf(theta);
+    if (st == 0.0f) pdf = 0.0f;
+    pdfOut = (pdf * (float)P.env_w * (float)P.env_h) / (PT_TWO_PI * PT_PI * st);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return v3(-st * cp, ct, -st * sp);
+}
+
+// sampling.glsl:186-248
+__device__ __forceinline__ void SampleOneLight(const Params& P, const Light& light, V3 scatterPos, LightSample& ls,
+                                               Rng& rng) {
+    const int type = (int)light.type;
+    if (type == QUAD_LIGHT) {
+        float r1 = rng.next();
+        float r2 = rng.next();
+        V3 lightSurfacePos = light.position + light.u * r1 + light.v * r2;
+        ls.direction = lightSurfacePos - scatterPos;
+        ls.dist = length(ls.direction);
+        float distSq = ls.dist * ls.dist;
+        ls.direction = ls.direction / ls.dist;
+        ls.normal = normalize(cross(light.u, light.v));
+        ls.emission = light.emission * (float)P.num_lights;
+        ls.pdf = distSq / (light.area * fabsf(dot(ls.normal, ls.direction)));
+    } else if (type == SPHERE_LIGHT) {
+        float r1 = rng.next();
+        float r2 = rng.next();
+        V3 c2s = scatterPos - light.position;
+        float distToSphereCenter = length(c2s);
+        c2s = c2s / distToSphereCenter;
+        V3 sampledDir = UniformSampleHemisphere(r1, r2);
+        V3 T, B;
+        Onb(c2s, T, B);
+        sampledDir = T * sampledDir.x + B * sampledDir.y + c2s * sampledDir.z;
+        V3 lightSurfacePos = light.position + sampledDir * light.radius;
+        ls.direction = lightSurfacePos - scatterPos;
+        ls.dist = length(ls.direction);
+        float distSq = ls.dist * ls.dist;
+        ls.direction = ls.direction / ls.dist;
+        ls.normal = normalize(lightSurfacePos - light.position);
+        ls.emission = light.emission * (float)P.num_lights;
+        ls.pdf = distSq / (light.area * 0.5f * fabsf(dot(ls.normal, ls.direction)));
+    } else {
+        ls.direction = normalize(light.position - v3(0.0f));
+        ls.normal = normalize(scatterPos - light.position);
+        ls.emission = light.emission * (float)P.num_lights;
+        ls.dist = PT_INF;
+        ls.pdf = 1.0f;
+    }
+}
+
+// Scattering at the current vertex for next-event estimation: Disney BSDF on
+// surfaces, Henyey-Greenstein phase function in media (pathtrace.glsl:181-188).
+__device__ __forceinline__ V3 ScatterEval(bool isSurface, const Material& mat, float eta, V3 V, V3 ffnormal,
+                                          float g, V3 L, float& pdf) {
+    if (isSurface) return DisneyEval(mat, eta, V, ffnormal, L, pdf);
+    float p = PhaseHG(dot(V, L), g);
+    pdf = p;
+    return v3(p);
+}
+
+// pathtrace.glsl:158-283.  INLINE: shadow rays traced here and the result
+// returned; otherwise the rays and their contributions go to `sr` and the
+// caller adds the unoccluded ones (same values, same order).
+template <int MEDIUM, bool ENV, bool INLINE>
+__device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp, V3 normal, V3 ffnormal,
+                                          const Material& mat, float eta, const Medium& medium, bool isSurface,
+                                          Rng& rng, uint2* stack, Counters& cnt, ShadowReq& sr) {
+    V3 Ld = v3(0.0f);
+    V3 Li = v3(0.0f);
+    const V3 scatterPos = fhp + normal * PT_EPS;
+    constexpr bool volmis = MEDIUM == 2;
+    const V3 V = -r.direction;
+    sr.n = 0;
+    sr.adds = 0;
+    sr.origin = scatterPos;
+    if (ENV) {
+        float lightPdf;
+        const V3 lightDir = SampleEnvMap(P, Li, lightPdf, rng);
+        const Ray shadowRay{scatterPos, lightDir};
+        if (volmis) {
+            Li = Li * EvalTransmittance(P, shadowRay, rng, stack, cnt);
+            float sfPdf;
+            const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, lightDir, sfPdf);
+            if (sfPdf > 0.0f) {
+                float misWeight = PowerHeuristic(lightPdf, sfPdf);
+                if (misWeight > 0.0f) Ld = Ld + misWeight * Li * sf * P.env_intensity / lightPdf;
+            }
+        } else {
+            float sfPdf = 0.0f;
+            V3 c = v3(0.0f);
+            bool adds = false;
+            auto contribution = [&]() {
+                const V3 sf = DisneyEval(mat, eta, V, ffnormal, lightDir, sfPdf);
+                if (sfPdf > 0.0f) {
+                    float misWeight = PowerHeuristic(lightPdf, sfPdf);
+                    if (misWeight > 0.0f) {
+                        c = misWeight * Li * sf * P.env_intensity / lightPdf;
+                        adds = true;
+                    }
+                }
+            };
+            if (INLINE) {
+                if (!AnyHit(P, shadowRay, PT_INF - PT_EPS, rng, stack, cnt)) {
+                    contribution();
+                    if (adds) Ld = Ld + c;
+                }
+            } else {
+                contribution();
+                sr.n |= 1;
+                sr.dir[0] = lightDir;
+                sr.maxd[0] = PT_INF - PT_EPS;
+                sr.contrib[0] = c;
+                if (adds) sr.adds |= 1;
+            }
+        }
+    }
+    if (P.flags & F_LIGHTS) {
+        LightSample ls;
+        const int index = (int)(rng.next() * (float)P.num_lights);
+        Light light;
+        if (index < P.num_lights) light = LoadLight(P.lights, index);
+        else {  // rand() == 1: one past the last light reads zeros (GL texelFetch out of range)
+            light.position = light.emission = light.u = light.v = v3(0.0f);
+            light.radius = light.area = light.type = 0.0f;
+        }
+        SampleOneLight(P, light, scatterPos, ls, rng);
+        Li = ls.emission;
+        if (dot(ls.direction, ls.normal) < 0.0f) {
+            const Ray shadowRay{scatterPos, ls.direction};
+            if (volmis) {
+                Li = Li * EvalTransmittance(P, shadowRay, rng, stack, cnt);
+                float sfPdf;
+                const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, ls.direction, sfPdf);
+                float misWeight = 1.0f;
+                if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
+                if (sfPdf > 0.0f) Ld = Ld + misWeight * sf * Li / ls.pdf;
+            } else {
+                float sfPdf = 0.0f;
+                V3 c = v3(0.0f);
+                bool adds = false;
+                auto contribution = [&]() {
+                    const V3 sf = DisneyEval(mat, eta, V, ffnormal, ls.direction, sfPdf);
+                    float misWeight = 1.0f;
+                    if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
+                    if (sfPdf > 0.0f) {
+                        c = misWeight * Li * sf / ls.pdf;
+                        adds = true;
+                    }
+                };
+                if (INLINE) {
+                    if (!AnyHit(P, shadowRay, ls.dist - PT_EPS, rng, stack, cnt)) {
+                        contribution();
+                        if (adds) Ld = Ld + c;
+                    }
+                } else {
+                    contribution();
+                    sr.n |= 2;
+                    sr.dir[1] = ls.direction;
+                    sr.maxd[1] = ls.dist - PT_EPS;
+                    sr.contrib[1] = c;
+                    if (adds) sr.adds |= 2;
+                }
+            }
+        }
+    }
+    return Ld;
+}
+
+// radiance += Ld * T, with the rounding fixed (one fused multiply-add per
+// channel) so that the inline and the deferred forms agree to the bit.
+__device__ __forceinline__ V3 AddScaled(V3 radiance, V3 Ld, V3 T) {
+    return v3(__fmaf_rn(Ld.x, T.x, radiance.x), __fmaf_rn(Ld.y, T.y, radiance.y), __fmaf_rn(Ld.z, T.z, radiance.z));
+}
+
+// Ld from the resolved shadow rays of a ShadowReq (env first, then light).
+__device__ __forceinline__ V3 ResolveShadow(const ShadowReq& sr, bool occ_env, bool occ_light) {
+    V3 Ld = v3(0.0f);
+    if ((sr.adds & 1) && !occ_env) Ld = Ld + sr.contrib[0];
+    if ((sr.adds & 2) && !occ_light) Ld = Ld + sr.contrib[1];
+    return Ld;
+}
+
+// One iteration of PathTrace's loop (pathtrace.glsl:301-473) for the hit in
+// `hr`.  Returns true if the path continues with ps.r (depth incremented).
+// With INLINE false, a pending next-event estimate is left in `sr`
+// (sr.n != 0): the caller adds ResolveShadow(...) * sr.T to the radiance
+// before anything else touches the path.
+template <int MEDIUM, bool ENV, bool INLINE>
+__device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const HitRecord& hr, ShadowReq& sr,
+                                          uint2* stack, Counters& cnt) {
+    const uint32_t F = P.flags;
+    sr.n = 0;
+    if (!hr.hit) {
+        if ((F & F_BACKGROUND) && ps.depth == 0) ps.alpha = 0.0f;
+        if (!((F & F_HIDE_EMITTERS) && !(ps.depth > 0))) {
+            if (F & F_UNIFORM_LIGHT) {
+                ps.radiance = ps.radiance + v3(P.uniform_light[0], P.uniform_light[1], P.uniform_light[2]) * ps.throughput;
+            } else if (ENV) {
+                float envPdf;
+                V3 envCol = EvalEnvMap(P, ps.r, envPdf);
+                float misWeight = 1.0f;
+                if (ps.depth > 0) misWeight = PowerHeuristic(ps.scatterPdf, envPdf);
+                if (MEDIUM == 1 && !ps.surfaceScatter) misWeight = 1.0f;
+                if (misWeight > 0.0f) ps.radiance = ps.radiance + misWeight * envCol * ps.throughput * P.env_intensity;
+            }
+        }
+        return false;
+    }
+    const V3 fhp = ps.r.origin + ps.r.direction * hr.t;
+    V3 normal = v3(0.0f), ffnormal = v3(0.0f);
+    if (hr.prim >= 0) {
+        HitNormal(P, hr, ps.r, normal, ffnormal);
+        ps.matID = hr.mat;
+    }
+    Material mat;
+    float eta;
+    GetMaterial(P, ps.matID, ps.depth, ps.prevRough, normal, ps.r, mat, eta);
+    ps.prevRough = mat.roughness;
+    ps.radiance = ps.radiance + mat.emission * ps.throughput;
+    if ((F & F_LIGHTS) && hr.isEmitter) {
+        float misWeight = 1.0f;
+        if (ps.depth > 0) misWeight = PowerHeuristic(ps.scatterPdf, hr.lightPdf);
+        if (MEDIUM == 1 && !ps.surfaceScatter) misWeight = 1.0f;
+        ps.radiance = ps.radiance + misWeight * hr.lightEmission * ps.throughput;
+        return false;
+    }
+    if (ps.depth == P.max_depth) return false;
+    bool mediumSampled = false;
+    V3 scatterL = v3(0.0f);
+    if (MEDIUM) {
+        ps.surfaceScatter = false;
+        if (ps.inMedium) {
+            if (ps.medium.type == MEDIUM_ABSORB) {
+                ps.throughput = ps.throughput * vexp(-(v3(1.0f) - ps.medium.color) * hr.t * ps.medium.density);
+            } else if (ps.medium.type == MEDIUM_EMISSIVE) {
+                ps.radiance = ps.radiance + ps.medium.color * hr.t * ps.medium.density * ps.throughput;
+            } else {
+                float scatterDist = fminf(-logf(ps.rng.next()) / ps.medium.density, hr.t);
+                mediumSampled = scatterDist < hr.t;
+                if (mediumSampled) {
+                    ps.throughput = ps.throughput * ps.medium.color;
+                    ps.r.origin = ps.r.origin + ps.r.direction * scatterDist;
+                    const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, ps.r.origin, normal, ffnormal, mat, eta,
+                                                                   ps.medium, false, ps.rng, stack, cnt, sr);
+                    if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
+                    else sr.T = ps.throughput;
+                    float h1 = ps.rng.next();
+                    float h2 = ps.rng.next();
+                    V3 scatterDir = SampleHG(-ps.r.direction, ps.medium.anisotropy, h1, h2);
+                    ps.scatterPdf = PhaseHG(dot(-ps.r.direction, scatterDir), ps.medium.anisotropy);
+                    ps.r.direction = scatterDir;
+                }
+            }
+        }
+    }
+    if (!mediumSampled) {
+        if ((F & F_ALPHA_TEST) && AlphaSkip(mat, ps.rng)) {
+            scatterL = ps.r.direction;
+            ps.depth--;
+        } else {
+            ps.surfaceScatter = true;
+            const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, fhp, normal, ffnormal, mat, eta, ps.medium, true,
+                                                           ps.rng, stack, cnt, sr);
+            if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
+            else sr.T = ps.throughput;
+            const V3 f = DisneySample(mat, eta, -ps.r.direction, ffnormal, scatterL, ps.scatterPdf, ps.rng);
+            if (ps.scatterPdf > 0.0f) ps.throughput = ps.throughput * (f / ps.scatterPdf);
+            else return false;
+        }
+        ps.r.direction = scatterL;
+        ps.r.origin = fhp + ps.r.direction * PT_EPS;
+        if (MEDIUM) {
+            if (dot(ps.r.direction, normal) < 0.0f && mat.medium.type != MEDIUM_NONE) {
+                ps.inMedium = true;
+                ps.medium = mat.medium;
+            } else if (mat.medium.type != MEDIUM_NONE) ps.inMedium = false;
+        }
+    }
+    if ((F & F_RR) && ps.depth >= P.rr_depth) {
+        float q = fminf(maxc(ps.throughput) + 0.001f, 0.95f);
+        if (ps.rng.next() > q) return false;
+        ps.throughput = ps.throughput / q;
+    }
+    ps.depth++;
+    return true;
+}
+
+// tile.glsl:41-74 for pixel (px, py); the RNG is seeded with the
+// tile-local fragment position, as the tile viewport gives gl_FragCoord.
+__device__ __forceinline__ Ray CameraRay(const Params& P, int px, int py, int tx, int ty, Rng& rng) {
+    const int lx = px - tx * P.tile_w, ly = py - ty * P.tile_h;
+    const float invx = (float)P.tile_w / (float)P.width, invy = (float)P.tile_h / (float)P.height;
+    const float tcx = ((float)lx + 0.5f) / (float)P.tile_w, tcy = ((float)ly + 0.5f) / (float)P.tile_h;
+    const float offx = (float)tx * invx, offy = (float)ty * invy;
+    const float cx = offx * (1.0f - tcx) + (offx + invx) * tcx;
+    const float cy = offy * (1.0f - tcy) + (offy + invy) * tcy;
+    float r1 = 2.0f * rng.next();
+    float r2 = 2.0f * rng.next();
+    float jx = r1 < 1.0f ? sqrtf(r1) - 1.0f : 1.0f - sqrtf(2.0f - r1);
+    float jy = r2 < 1.0f ? sqrtf(r2) - 1.0f : 1.0f - sqrtf(2.0f - r2);
+    const float resx = (float)P.width, resy = (float)P.height;
+    jx = jx / (resx * 0.5f);
+    jy = jy / (resy * 0.5f);
+    float dx = (cx * 2.0f - 1.0f) + jx;
+    float dy = (cy * 2.0f - 1.0f) + jy;
+    const float scale = tanf(P.cam_fov * 0.5f);
+    dy *= resy / resx * scale;
+    dx *= scale;
+    const V3 right = v3(P.cam_right[0], P.cam_right[1], P.cam_right[2]);
+    const V3 up = v3(P.cam_up[0], P.cam_up[1], P.cam_up[2]);
+    const V3 fwd = v3(P.cam_fwd[0], P.cam_fwd[1], P.cam_fwd[2]);
+    const V3 pos = v3(P.cam_pos[0], P.cam_pos[1], P.cam_pos[2]);
+    const V3 rayDir = normalize(dx * right + dy * up + fwd);
+    const V3 focalPoint = P.cam_focal * rayDir;
+    const float cam_r1 = rng.next() * PT_TWO_PI;
+    const float cam_r2 = rng.next() * P.cam_aperture;
+    float s, c;
+    sincosf(cam_r1, &s, &c);
+    const V3 aperturePos = (c * right + s * up) * sqrtf(cam_r2);
+    const V3 finalDir = normalize(focalPoint - aperturePos);
+    return Ray{pos + aperturePos, finalDir};
+}
+
+// The start of a path: tile.glsl's seed and camera ray, PathTrace's initial
+// state (pathtrace.glsl:287-299).
+__device__ __forceinline__ void StartPath(const Params& P, int px, int py, uint32_t frame, PathState& ps) {
+    const int tx = px / P.tile_w, ty = py / P.tile_h;
+    ps.rng.init((uint32_t)(px - tx * P.tile_w), (uint32_t)(py - ty * P.tile_h), frame);
+    ps.r = CameraRay(P, px, py, tx, ty, ps.rng);
+    ps.throughput = v3(1.0f);
+    ps.radiance = v3(0.0f);
+    ps.alpha = 1.0f;
+    ps.depth = 0;
+    ps.matID = 0;
+    ps.prevRough = 0.0f;
+    ps.scatterPdf = 0.0f;
+    ps.inMedium = false;
+    ps.surfaceScatter = false;
+    ps.medium.type = 0;
+    ps.medium.density = 0.0f;
+    ps.medium.color = v3(0.0f);
+    ps.medium.anisotropy = 0.0f;
+}
+
+// Frame number of pass `pass` for the tile containing (px, py), as the
+// reference's tile state machine assigns them (Renderer.cpp:745-783).
+__device__ __forceinline__ uint32_t FrameNumber(const Params& P, const RenderWork& W, int pass, int px, int py) {
+    if (W.tile_frame >= 0) return (uint32_t)W.tile_frame;
+    const int tx = px / P.tile_w, ty = py / P.tile_h;
+    return (uint32_t)(2 + pass * P.ntx * P.nty + (P.nty - 1 - ty) * P.ntx + tx);
+}
+
+__device__ __forceinline__ void add_counters(const Params& P, uint32_t closest, uint32_t shadow, uint32_t paths) {
+    const unsigned mask = __activemask();
+    closest = __reduce_add_sync(mask, closest);
+    shadow = __reduce_add_sync(mask, shadow);
+    paths = __reduce_add_sync(mask, paths);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+        if (closest) atomicAdd(P.counters + 0, (unsigned long long)closest);
+        if (shadow) atomicAdd(P.counters + 1, (unsigned long long)shadow);
+        if (paths) atomicAdd(P.counters + 2, (unsigned long long)paths);
+    }
+}
+
+}  // namespace ptgb

@@ -1,0 +1,423 @@
+// pt_wavefront.cu - the wavefront form of the integrator (sm_103a).
+//
+// A batch is every pixel of the work rectangle times a range of sample
+// passes: one path per (pixel, pass), its state kept in HBM as
+// structure-of-arrays float4/int4/uint4 records.  Per bounce:
+//   extend  closest-hit queries for the paths in the active queue
+//   shade   ShadeStep (pt_integrator.cuh) for each of them: survivors are
+//           appended to the next queue, next-event estimates to the shadow
+//           queue
+//   shadow  any-hit queries of the shadow queue, radiance += Ld * T
+// then `resolve` adds each path's radiance into the accumulation buffer,
+// pixel by pixel in pass order, which is the order the megakernel (and the
+// reference's per-pass accumulation, tile.glsl:70-74) adds them in: both
+// forms produce the same accumulation bit for bit.
+// The stage kernels are persistent grid-stride loops over a device-side
+// count, so a whole batch (generate, max_depth+1 bounces, resolve) needs no
+// host round trip and is captured as one CUDA graph.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pt_cuda.h"
+#include "pt_integrator.cuh"
+#include "pt_wavefront.h"
+
+namespace ptgb {
+
+namespace {
+
+struct WfView {  // device pointers of WavefrontBuffers, by value
+    float4 *o, *d, *T, *L, *med;
+    uint4* rng;
+    int4* misc;
+    float4 *h0, *h2;
+    int4* h1;
+    float4 *so, *sd0, *sd1, *sc0, *sc1, *sT;
+    float4* rad;
+    int* q[2];
+    int* qs;
+    int* counts;  // [0], [1] extension queues, [2] shadow queue
+};
+
+__device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps) {
+    const float4 o = B.o[i], d = B.d[i], T = B.T[i], L = B.L[i], m = B.med[i];
+    const uint4 g = B.rng[i];
+    const int4 misc = B.misc[i];
+    ps.r.origin = v3(o.x, o.y, o.z);
+    ps.alpha = o.w;
+    ps.r.direction = v3(d.x, d.y, d.z);
+    ps.scatterPdf = d.w;
+    ps.throughput = v3(T.x, T.y, T.z);
+    ps.prevRough = T.w;
+    ps.radiance = v3(L.x, L.y, L.z);
+    ps.medium.density = L.w;
+    ps.medium.color = v3(m.x, m.y, m.z);
+    ps.medium.anisotropy = m.w;
+    ps.rng.x = g.x; ps.rng.y = g.y; ps.rng.z = g.z; ps.rng.w = g.w;
+    ps.depth = misc.x;
+    ps.matID = misc.y;
+    ps.inMedium = misc.z & 1;
+    ps.surfaceScatter = (misc.z >> 1) & 1;
+    ps.medium.type = misc.z >> 8;
+}
+
+__device__ __forceinline__ void store_path(const WfView& B, int i, const PathState& ps) {
+    B.o[i] = make_float4(ps.r.origin.x, ps.r.origin.y, ps.r.origin.z, ps.alpha);
+    B.d[i] = make_float4(ps.r.direction.x, ps.r.direction.y, ps.r.direction.z, ps.scatterPdf);
+    B.T[i] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.prevRough);
+    B.L[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.medium.density);
+    B.med[i] = make_float4(ps.medium.color.x, ps.medium.color.y, ps.medium.color.z, ps.medium.anisotropy);
+    B.rng[i] = make_uint4(ps.rng.x, ps.rng.y, ps.rng.z, ps.rng.w);
+    B.misc[i] = make_int4(ps.depth, ps.matID,
+                          (ps.inMedium ? 1 : 0) | (ps.surfaceScatter ? 2 : 0) | (ps.medium.type << 8), 0);
+}
+
+// Append to a queue with one atomic per warp.
+__device__ __forceinline__ void push(int* queue, int* count, int value, bool pred) {
+    const unsigned mask = __ballot_sync(__activemask(), pred);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(__activemask(), base, leader);
+    if (pred) queue[base + __popc(mask & ((1u << lane) - 1))] = value;
+}
+
+__global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfView B, int first_pass, int npass) {
+    const int npix = W.w * W.h;
+    const int n = npix * npass;
+    uint32_t paths = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int pix = i % npix, k = i / npix;
+        const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+        PathState ps;
+        StartPath(P, px, py, FrameNumber(P, W, first_pass + k, px, py), ps);
+        store_path(B, i, ps);
+        B.q[0][i] = i;
+        ++paths;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        B.counts[0] = n;
+        B.counts[1] = 0;
+        B.counts[2] = 0;
+    }
+    add_counters(P, 0, 0, paths);
+}
+
+__global__ void __launch_bounds__(128) wf_extend(Params P, WfView B, int in) {
+    uint2 stack[kStackSize];
+    const int n = B.counts[in];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        B.counts[in ^ 1] = 0;  // the next queue and the shadow queue start empty
+        B.counts[2] = 0;
+    }
+    Counters cnt{0, 0};
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = B.q[in][j];
+        const float4 o = B.o[i], d = B.d[i];
+        const int depth = B.misc[i].x;
+        const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
+        HitRecord hr;
+        TraceClosest(P, r, depth, hr, stack, cnt, false);
+        B.h0[i] = make_float4(hr.t, hr.u, hr.v, hr.w);
+        B.h1[i] = make_int4(hr.prim, hr.inst, hr.mat, (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 : 0));
+        B.h2[i] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
+template <int MEDIUM, bool ENV, bool INLINE>
+__global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
+    uint2 stack[INLINE ? kStackSize : 1];
+    const int n = B.counts[in];
+    Counters cnt{0, 0};
+    for (int j0 = blockIdx.x * blockDim.x; j0 < n; j0 += gridDim.x * blockDim.x) {
+        const int j = j0 + threadIdx.x;
+        const bool valid = j < n;
+        bool cont = false, shadow = false;
+        int i = 0;
+        if (valid) {
+            i = B.q[in][j];
+            PathState ps;
+            load_path(B, i, ps);
+            HitRecord hr;
+            const float4 h0 = B.h0[i], h2 = B.h2[i];
+            const int4 h1 = B.h1[i];
+            hr.t = h0.x; hr.u = h0.y; hr.v = h0.z; hr.w = h0.w;
+            hr.prim = h1.x; hr.inst = h1.y; hr.mat = h1.z;
+            hr.hit = h1.w & 1;
+            hr.isEmitter = (h1.w >> 1) & 1;
+            hr.lightEmission = v3(h2.x, h2.y, h2.z);
+            hr.lightPdf = h2.w;
+            ShadowReq sr;
+            cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt);
+            if (cont && ps.depth > 65536) {  // alpha pass-through loops are bounded (pt_kernels.cu)
+                flag_status(P.status, PT_ERR_TIMEOUT);
+                cont = false;
+            }
+            store_path(B, i, ps);
+            shadow = !INLINE && sr.n != 0;
+            if (shadow) {
+                const int bits = sr.n | (sr.adds << 2) | (cont ? 0 : 16);
+                B.so[i] = make_float4(sr.origin.x, sr.origin.y, sr.origin.z, __int_as_float(bits));
+                if (sr.n & 1) {
+                    B.sd0[i] = make_float4(sr.dir[0].x, sr.dir[0].y, sr.dir[0].z, sr.maxd[0]);
+                    B.sc0[i] = make_float4(sr.contrib[0].x, sr.contrib[0].y, sr.contrib[0].z, 0.0f);
+                }
+                if (sr.n & 2) {
+                    B.sd1[i] = make_float4(sr.dir[1].x, sr.dir[1].y, sr.dir[1].z, sr.maxd[1]);
+                    B.sc1[i] = make_float4(sr.contrib[1].x, sr.contrib[1].y, sr.contrib[1].z, 0.0f);
+                }
+                B.sT[i] = make_float4(sr.T.x, sr.T.y, sr.T.z, 0.0f);
+            } else if (!cont) {
+                B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
+            }
+        }
+        push(B.q[in ^ 1], B.counts + (in ^ 1), i, valid && cont);
+        push(B.qs, B.counts + 2, i, valid && shadow);
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
+__global__ void __launch_bounds__(128) wf_shadow(Params P, WfView B) {
+    uint2 stack[kStackSize];
+    const int n = B.counts[2];
+    Counters cnt{0, 0};
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = B.qs[j];
+        const float4 so = B.so[i];
+        const int bits = __float_as_int(so.w);
+        ShadowReq sr;
+        sr.n = bits & 3;
+        sr.adds = (bits >> 2) & 3;
+        const V3 origin = v3(so.x, so.y, so.z);
+        Rng rng;  // the deferred form is used only when AnyHit draws no random numbers
+        rng.x = rng.y = rng.z = rng.w = 0;
+        bool occ0 = false, occ1 = false;
+        if (sr.n & 1) {
+            const float4 d = B.sd0[i];
+            const float4 c = B.sc0[i];
+            sr.contrib[0] = v3(c.x, c.y, c.z);
+            occ0 = AnyHit(P, Ray{origin, v3(d.x, d.y, d.z)}, d.w, rng, stack, cnt);
+        }
+        if (sr.n & 2) {
+            const float4 d = B.sd1[i];
+            const float4 c = B.sc1[i];
+            sr.contrib[1] = v3(c.x, c.y, c.z);
+            occ1 = AnyHit(P, Ray{origin, v3(d.x, d.y, d.z)}, d.w, rng, stack, cnt);
+        }
+        const float4 T = B.sT[i];
+        const V3 Ld = ResolveShadow(sr, occ0, occ1);
+        float4 L = B.L[i];
+        const V3 rad = AddScaled(v3(L.x, L.y, L.z), Ld, v3(T.x, T.y, T.z));
+        L.x = rad.x;
+        L.y = rad.y;
+        L.z = rad.z;
+        B.L[i] = L;
+        if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
+__global__ void __launch_bounds__(256) wf_resolve(Params P, RenderWork W, WfView B, int npass) {
+    const int npix = W.w * W.h;
+    for (int pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
+        const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+        float4* out = P.accum + (size_t)py * P.width + px;
+        float4 acc = *out;
+        for (int k = 0; k < npass; ++k) {
+            const float4 r = B.rad[(size_t)k * npix + pix];
+            acc.x += r.x;
+            acc.y += r.y;
+            acc.z += r.z;
+            acc.w += r.w;
+        }
+        *out = acc;
+    }
+}
+
+WfView view_of(const WavefrontBuffers& wb) {
+    WfView v;
+    v.o = wb.o; v.d = wb.d; v.T = wb.T; v.L = wb.L; v.med = wb.med;
+    v.rng = wb.rng; v.misc = wb.misc;
+    v.h0 = wb.h0; v.h1 = wb.h1; v.h2 = wb.h2;
+    v.so = wb.so; v.sd0 = wb.sd0; v.sd1 = wb.sd1; v.sc0 = wb.sc0; v.sc1 = wb.sc1; v.sT = wb.sT;
+    v.rad = wb.rad;
+    v.q[0] = wb.q[0]; v.q[1] = wb.q[1]; v.qs = wb.qs;
+    v.counts = wb.counts;
+    return v;
+}
+
+template <int MEDIUM, bool ENV, bool INLINE>
+cudaError_t launch_shade(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
+    wf_shade<MEDIUM, ENV, INLINE><<<grid, block, 0, s>>>(p, v, in);
+    return cudaGetLastError();
+}
+
+cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
+    const int medium = (p.flags & F_MEDIUM) ? ((p.flags & F_VOL_MIS) ? 2 : 1) : 0;
+    const bool env = (p.flags & F_ENVMAP) != 0;
+    // AnyHit draws random numbers for alpha-tested materials without media
+    // (anyhit.glsl:118-141) and transmittance does with VOL_MIS: those keep
+    // the shadow rays inline so every path draws the reference's sequence
+    const bool inl = medium == 2 || ((p.flags & F_ALPHA_TEST) && medium == 0);
+    switch ((medium * 2 + (env ? 1 : 0)) * 2 + (inl ? 1 : 0)) {
+        case 0: return launch_shade<0, false, false>(p, v, in, grid, block, s);
+        case 1: return launch_shade<0, false, true>(p, v, in, grid, block, s);
+        case 2: return launch_shade<0, true, false>(p, v, in, grid, block, s);
+        case 3: return launch_shade<0, true, true>(p, v, in, grid, block, s);
+        case 4: return launch_shade<1, false, false>(p, v, in, grid, block, s);
+        case 5: return launch_shade<1, false, true>(p, v, in, grid, block, s);
+        case 6: return launch_shade<1, true, false>(p, v, in, grid, block, s);
+        case 7: return launch_shade<1, true, true>(p, v, in, grid, block, s);
+        case 9: return launch_shade<2, false, true>(p, v, in, grid, block, s);
+        default: return launch_shade<2, true, true>(p, v, in, grid, block, s);
+    }
+}
+
+}  // namespace
+
+size_t wavefront_bytes_per_path() { return 17 * 16 + 3 * sizeof(int); }
+
+cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity) {
+    wavefront_free(wb);
+    wb.capacity = capacity;
+    const size_t n = (size_t)capacity;
+    float4** f4[] = {&wb.o, &wb.d, &wb.T, &wb.L, &wb.med, &wb.h0, &wb.h2, &wb.so, &wb.sd0, &wb.sd1,
+                     &wb.sc0, &wb.sc1, &wb.sT, &wb.rad};
+    for (float4** p : f4) {
+        cudaError_t e = cudaMalloc((void**)p, n * sizeof(float4));
+        if (e != cudaSuccess) { wavefront_free(wb); return e; }
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&wb.rng, n * sizeof(uint4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.misc, n * sizeof(int4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.h1, n * sizeof(int4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.q[0], n * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.q[1], n * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.qs, n * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.counts, 4 * sizeof(int))) != cudaSuccess) {
+        wavefront_free(wb);
+        return e;
+    }
+    return cudaSuccess;
+}
+
+void wavefront_free(WavefrontBuffers& wb) {
+    void* ptrs[] = {wb.o, wb.d, wb.T, wb.L, wb.med, wb.h0, wb.h2, wb.so, wb.sd0, wb.sd1, wb.sc0, wb.sc1, wb.sT,
+                    wb.rad, wb.rng, wb.misc, wb.h1, wb.q[0], wb.q[1], wb.qs, wb.counts};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (wb.graph_exec) cudaGraphExecDestroy(wb.graph_exec);
+    wb = WavefrontBuffers{};
+}
+
+// Enqueue one batch: passes [first_pass, first_pass + npass) of the pixels of W.
+static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const WavefrontBuffers& wb, int first_pass,
+                                 int npass, int iterations, const WavefrontTuning& t, cudaStream_t s) {
+    const WfView v = view_of(wb);
+    const int n = W.w * W.h * npass;
+    const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
+    wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, first_pass, npass);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    for (int it = 0; it < iterations; ++it) {
+        const int in = it & 1;
+        wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
+        wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
+                             bool use_graph, cudaStream_t s) {
+    if (W.w <= 0 || W.h <= 0 || W.num_passes <= 0) return cudaSuccess;
+    const int npix = W.w * W.h;
+    const int per_batch = std::max(1, std::min(W.num_passes, wb.capacity / npix));
+    // max_depth+1 extension rounds finish every path unless alpha
+    // pass-through keeps some at the same depth; those run extra rounds.
+    const int iterations = p.max_depth + 1;
+    const bool may_linger = (p.flags & F_ALPHA_TEST) != 0;
+    const WfView v = view_of(wb);
+    for (int first = W.first_pass; first < W.first_pass + W.num_passes; first += per_batch) {
+        const int npass = std::min(per_batch, W.first_pass + W.num_passes - first);
+        cudaError_t e;
+        if (use_graph) {
+            cudaGraph_t g = nullptr;
+            if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+            cudaError_t ce = enqueue_batch(p, W, wb, first, npass, iterations, t, s);
+            e = cudaStreamEndCapture(s, &g);
+            if (ce != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return ce;
+            }
+            if (e != cudaSuccess) return e;
+            bool updated = false;
+            if (wb.graph_exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(wb.graph_exec, g, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();
+                    cudaGraphExecDestroy(wb.graph_exec);
+                    wb.graph_exec = nullptr;
+                }
+            }
+            if (!updated) {
+                e = cudaGraphInstantiate(&wb.graph_exec, g, 0);
+                if (e != cudaSuccess) {
+                    cudaGraphDestroy(g);
+                    wb.graph_exec = nullptr;
+                    return e;
+                }
+            }
+            cudaGraphDestroy(g);
+            if ((e = cudaGraphLaunch(wb.graph_exec, s)) != cudaSuccess) return e;
+        } else if ((e = enqueue_batch(p, W, wb, first, npass, iterations, t, s)) != cudaSuccess) {
+            return e;
+        }
+        if (may_linger) {
+            // bounded host loop over the remaining alpha pass-through paths
+            for (int it = iterations, guard = 0; guard < 65536; ++it, ++guard) {
+                int count = 0;
+                if ((e = cudaMemcpyAsync(&count, wb.counts + (it & 1), sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+                    cudaSuccess)
+                    return e;
+                if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+                if (count == 0) break;
+                const int in = it & 1;
+                wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in);
+                if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
+                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v);
+                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            }
+        }
+        const int res_grid = std::min((npix + 255) / 256, t.resident_blocks_256);
+        wf_resolve<<<res_grid, 256, 0, s>>>(p, W, v, npass);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    int b_ext = 0, b_shade = 0, b_shadow = 0, b256 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_ext, wf_extend, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shade, wf_shade<0, false, false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shadow, wf_shadow, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b256, wf_resolve, 256, 0);
+    t.extend_block = t.shade_block = t.shadow_block = block;
+    t.extend_grid = sms * std::max(1, b_ext);
+    t.shade_grid = sms * std::max(1, b_shade);
+    t.shadow_grid = sms * std::max(1, b_shadow);
+    t.resident_blocks_256 = sms * std::max(1, b256);
+    return cudaSuccess;
+}
+
+}  // namespace ptgb

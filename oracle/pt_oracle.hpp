@@ -289,7 +289,7 @@ template <class R> struct Light { V3<R> position, emission, u, v; R radius, area
 
 // Counters of executed ray queries and traversal work.
 struct Counters {
-    uint64_t closest = 0, shadow = 0, nodes = 0, tris = 0, overflow = 0;
+    uint64_t closest = 0, shadow = 0, nodes = 0, tris = 0, overflow = 0, tri_hits = 0;
 };
 
 // ------------------------------------------------------------ textures
@@ -531,6 +531,7 @@ template <class R> inline bool ClosestHit(const Scene<R>& s, const Ray<R>& r, St
     state.fhp = r.origin + r.direction * t;
 
     if (h.prim >= 0) {  // closest_hit.glsl:227-263
+        cnt.tri_hits++;
         state.isEmitter = false;
         state.matID = h.matID;
         const int32_t* vi = s.d->vert_indices + 3 * (size_t)h.prim;
