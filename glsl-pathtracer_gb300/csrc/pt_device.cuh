@@ -366,7 +366,7 @@ __device__ __forceinline__ V3 EvalClearcoat(const Material& mat, V3 V, V3 L, V3 
 // weighted contribution (diffuse, dielectric, metal, glass, clearcoat).
 // Not inlined: it has three call sites per path vertex, and the copies
 // cost more in instruction-cache misses than the call does.
-__device__ __noinline__ V3 DisneyEval(const Material& mat, float eta, V3 V, V3 N, V3 L, float& pdf,
+static __device__ __noinline__ V3 DisneyEval(const Material& mat, float eta, V3 V, V3 N, V3 L, float& pdf,
                                          V3* lobeF = nullptr, float* lobePdf = nullptr) {
     pdf = 0.0f;
     V3 f = v3(0.0f);

@@ -148,7 +148,8 @@ __device__ __forceinline__ bool AlphaSkip(const Material& m, Rng& rng) {
 }
 
 // anyhit.glsl:25-216
-__device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack, Counters& cnt) {
+static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack,
+                                           Counters& cnt) {
     cnt.shadow++;
     if (P.flags & F_LIGHTS) {
         for (int i = 0; i < P.num_lights; i++) {
@@ -174,7 +175,7 @@ __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist
 
 // pathtrace.glsl:118-156 (OPT_MEDIUM && OPT_VOL_MIS); each segment is counted
 // as a shadow query.
-__device__ __noinline__ V3 EvalTransmittance(const Params& P, Ray r, Rng& rng, uint2* stack, Counters& cnt) {
+static __device__ __noinline__ V3 EvalTransmittance(const Params& P, Ray r, Rng& rng, uint2* stack, Counters& cnt) {
     V3 transmittance = v3(1.0f);
     int matID = 0;
     for (int depth = 0; depth < P.max_depth; depth++) {
