@@ -56,10 +56,9 @@ struct Counters {
 };
 
 // ------------------------------------------------------------ ClosestHit
-__device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int depth, HitRecord& hr, uint2* stack,
-                                             Counters& cnt, bool count_as_shadow) {
-    if (count_as_shadow) cnt.shadow++;
-    else cnt.closest++;
+// The analytic-light part of ClosestHit (closest_hit.glsl:30-86): returns the
+// nearest light distance (INF if none) and fills the light fields of hr.
+__device__ __forceinline__ float LightsClosest(const Params& P, const Ray& r, int depth, HitRecord& hr) {
     float t = PT_INF;
     hr.isEmitter = false;
     if ((P.flags & F_LIGHTS) && !((P.flags & F_HIDE_EMITTERS) && !(depth > 0))) {  // closest_hit.glsl:30-86
@@ -96,25 +95,35 @@ __device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int 
             }
         }
     }
-    TriHit h;
-    h.t = t;
-    h.prim = -1;
-    h.inst = -1;
-    h.mat = 0;
-    h.u = h.v = h.w = 0.0f;
-    traverse_closest<true>(P, P.tlas_root, prep_ray(r.origin, r.direction), h, stack, 0, -1, 0);
-    if (h.prim >= 0) {
-        t = h.t;
+    return t;
+}
+
+// The HitRecord of a finished closest-hit traversal (the end of
+// closest_hit.glsl:220-228): a triangle closer than the lights wins.
+__device__ __forceinline__ void FinishClosest(const Trav& s, float tLight, HitRecord& hr) {
+    float t = tLight;
+    if (s.prim >= 0) {
+        t = s.tmax;
         hr.isEmitter = false;
     }
     hr.hit = t != PT_INF;
     hr.t = t;
-    hr.prim = h.prim;
-    hr.inst = h.inst;
-    hr.mat = h.mat;
-    hr.u = h.u;
-    hr.v = h.v;
-    hr.w = h.w;
+    hr.prim = s.prim;
+    hr.inst = s.inst;
+    hr.mat = s.mat;
+    hr.u = s.u;
+    hr.v = s.v;
+    hr.w = s.w;
+}
+
+__device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int depth, HitRecord& hr, uint2* stack,
+                                             Counters& cnt, bool count_as_shadow) {
+    if (count_as_shadow) cnt.shadow++;
+    else cnt.closest++;
+    const float tl = LightsClosest(P, r, depth, hr);
+    Trav s;
+    trace_closest(s, P, r.origin, r.direction, tl, stack);
+    FinishClosest(s, tl, hr);
 }
 
 // Shading attributes of a triangle hit (closest_hit.glsl:224-247).
@@ -147,10 +156,8 @@ __device__ __forceinline__ bool AlphaSkip(const Material& m, Rng& rng) {
     return false;
 }
 
-// anyhit.glsl:25-216
-static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack,
-                                           Counters& cnt) {
-    cnt.shadow++;
+// The analytic-light part of AnyHit (anyhit.glsl:28-63).
+__device__ __forceinline__ bool LightsAny(const Params& P, const Ray& r, float maxDist) {
     if (P.flags & F_LIGHTS) {
         for (int i = 0; i < P.num_lights; i++) {
             const Light L = LoadLight(P.lights, i);
@@ -169,8 +176,16 @@ static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float 
             }
         }
     }
+    return false;
+}
+
+// anyhit.glsl:25-216
+static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack,
+                                           Counters& cnt) {
+    cnt.shadow++;
+    if (LightsAny(P, r, maxDist)) return true;
     const bool alpha = (P.flags & F_ALPHA_TEST) && !(P.flags & F_MEDIUM);
-    return traverse_any<true>(P, P.tlas_root, prep_ray(r.origin, r.direction), maxDist, stack, 0, 0, alpha, rng);
+    return trace_any(P, r.origin, r.direction, maxDist, alpha, rng, stack);
 }
 
 // pathtrace.glsl:118-156 (OPT_MEDIUM && OPT_VOL_MIS); each segment is counted

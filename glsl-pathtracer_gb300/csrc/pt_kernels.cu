@@ -60,18 +60,12 @@ __global__ void __launch_bounds__(128) trace_closest_kernel(Params P, const pt_r
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const pt_ray rr = rays[i];
-    TriHit h;
-    h.t = PT_INF;
-    h.prim = -1;
-    h.inst = -1;
-    h.u = h.v = 0.0f;
-    traverse_closest<true>(P, P.tlas_root,
-                           prep_ray(v3(rr.origin[0], rr.origin[1], rr.origin[2]),
-                                    v3(rr.direction[0], rr.direction[1], rr.direction[2])),
-                           h, stack, 0, -1, 0);
+    Trav h;
+    trace_closest(h, P, v3(rr.origin[0], rr.origin[1], rr.origin[2]),
+                  v3(rr.direction[0], rr.direction[1], rr.direction[2]), PT_INF, stack);
     pt_hit o;
     if (h.prim >= 0) {
-        o.t = h.t; o.u = h.u; o.v = h.v; o.prim_id = h.prim; o.inst_id = h.inst;
+        o.t = h.tmax; o.u = h.u; o.v = h.v; o.prim_id = h.prim; o.inst_id = h.inst;
     } else {
         o.t = PT_INF; o.u = o.v = 0.0f; o.prim_id = -1; o.inst_id = -1;
     }
@@ -88,10 +82,8 @@ __global__ void __launch_bounds__(128) trace_shadow_kernel(Params P, const pt_ra
     Rng rng;
     rng.init((uint32_t)i, 0u, 0u);
     const bool alpha = (P.flags & F_ALPHA_TEST) && !(P.flags & F_MEDIUM);
-    occ[i] = traverse_any<true>(P, P.tlas_root,
-                                prep_ray(v3(rr.origin[0], rr.origin[1], rr.origin[2]),
-                                         v3(rr.direction[0], rr.direction[1], rr.direction[2])),
-                                maxd[i], stack, 0, 0, alpha, rng)
+    occ[i] = trace_any(P, v3(rr.origin[0], rr.origin[1], rr.origin[2]),
+                       v3(rr.direction[0], rr.direction[1], rr.direction[2]), maxd[i], alpha, rng, stack)
                  ? 1
                  : 0;
 }

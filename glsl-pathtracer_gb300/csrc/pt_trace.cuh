@@ -2,12 +2,23 @@
 //
 // A node fetch is five 128-bit loads; the eight child boxes are slab-tested
 // against the ray and the hits become a 32-bit mask: bits 24-31 internal
-// children in octant order, bits 0-23 leaf primitives.  Node groups (child
-// base, remaining hit bits | imask) go to a per-thread stack; leaf triangles
-// are tested at once.  The triangle test repeats the reference's arithmetic
-// operation for operation, without fused multiply-adds
-// (closest_hit.glsl:128-143), so hit decisions and distances equal the
-// oracle's bit for bit.
+// children in octant order, bits 0-23 leaf primitives (triangles in a BLAS,
+// instances in the TLAS).
+//
+// Traversal is a state machine that does one unit of work per step -- test
+// one triangle, enter one instance, intersect one node, or pop the stack --
+// so that the threads of a warp stay in one loop whatever level and stage
+// each ray is at, and a thread whose ray finished can take a new one at once
+// (the persistent kernels of pt_wavefront.cu).  Both levels of the
+// reference's two-level BVH run in the same loop: entering an instance keeps
+// the TLAS node group and the remaining instance bits in registers and marks
+// the stack height; leaving the BLAS restores them.
+//
+// The triangle test repeats the reference's arithmetic operation for
+// operation, without fused multiply-adds (closest_hit.glsl:128-143), so hit
+// decisions and distances equal the oracle's bit for bit.  Most triangles
+// are rejected before the three divisions, by tests that reject exactly the
+// triangles the full test would (see tri_test).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,7 +57,11 @@ __device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
     return r;
 }
 
-__device__ __forceinline__ float qbyte(uint32_t w, int j) { return __uint2float_rn((w >> (8 * j)) & 0xffu); }
+// Byte j of w as a float, without the (quarter-rate) integer conversion:
+// the byte becomes the low mantissa bits of 2^23, which is then subtracted.
+__device__ __forceinline__ float qbyte(uint32_t w, int j) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j)) - 8388608.0f;
+}
 
 // Slab test of the eight children of wide node `idx`; returns the hit mask.
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
@@ -94,36 +109,52 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
     return hits;
 }
 
-// Triangle test of closest_hit.glsl:128-143 with the reference's operation
-// order and no contraction: returns the barycentrics and distance.
-__device__ __forceinline__ bool tri_test(const TRay& r, const float4* __restrict__ tris, int t, float& u, float& v,
-                                         float& tt, float& w, int& prim) {
+// Triangle test of closest_hit.glsl:128-143 (accept when u, v, t and
+// w = 1-u-v are all >= 0 and t < tmax) with the reference's operation order
+// and no contraction.  The numerators U, V, T and det are computed first;
+// with det made positive (an exact sign flip of all four) a triangle is
+// rejected before dividing when
+//   U, V or T < -det * 1e-30   the quotient is negative and not so small
+//                              that it would round to zero,
+//   U + V > det * (1 + 1e-6)   u + v exceeds 1 by far more than the
+//                              rounding of (1 - u) - v, so w < 0,
+//   T > det * tmax * (1 + 1e-6)  t rounds to above tmax;
+// each of these implies the full test fails, so the accepted set is unchanged.
+__device__ __forceinline__ bool tri_test(const TRay& r, const float4* __restrict__ tris, int t, float tmax, float& u,
+                                         float& v, float& tt, float& w, int& prim) {
     const float4 a = __ldg(tris + 3 * (size_t)t), b = __ldg(tris + 3 * (size_t)t + 1),
                  c = __ldg(tris + 3 * (size_t)t + 2);
-    prim = __float_as_int(a.w);
     // e0 = b, e1 = c (precomputed v1-v0, v2-v0)
     const float pvx = __fsub_rn(__fmul_rn(r.d.y, c.z), __fmul_rn(r.d.z, c.y));
     const float pvy = __fsub_rn(__fmul_rn(r.d.z, c.x), __fmul_rn(r.d.x, c.z));
     const float pvz = __fsub_rn(__fmul_rn(r.d.x, c.y), __fmul_rn(r.d.y, c.x));
-    const float det = __fadd_rn(__fadd_rn(__fmul_rn(b.x, pvx), __fmul_rn(b.y, pvy)), __fmul_rn(b.z, pvz));
+    float det = __fadd_rn(__fadd_rn(__fmul_rn(b.x, pvx), __fmul_rn(b.y, pvy)), __fmul_rn(b.z, pvz));
     const float tvx = __fsub_rn(r.o.x, a.x), tvy = __fsub_rn(r.o.y, a.y), tvz = __fsub_rn(r.o.z, a.z);
     const float qvx = __fsub_rn(__fmul_rn(tvy, b.z), __fmul_rn(tvz, b.y));
     const float qvy = __fsub_rn(__fmul_rn(tvz, b.x), __fmul_rn(tvx, b.z));
     const float qvz = __fsub_rn(__fmul_rn(tvx, b.y), __fmul_rn(tvy, b.x));
-    const float U = __fadd_rn(__fadd_rn(__fmul_rn(tvx, pvx), __fmul_rn(tvy, pvy)), __fmul_rn(tvz, pvz));
-    const float Vv = __fadd_rn(__fadd_rn(__fmul_rn(r.d.x, qvx), __fmul_rn(r.d.y, qvy)), __fmul_rn(r.d.z, qvz));
-    const float T = __fadd_rn(__fadd_rn(__fmul_rn(c.x, qvx), __fmul_rn(c.y, qvy)), __fmul_rn(c.z, qvz));
+    float U = __fadd_rn(__fadd_rn(__fmul_rn(tvx, pvx), __fmul_rn(tvy, pvy)), __fmul_rn(tvz, pvz));
+    float Vv = __fadd_rn(__fadd_rn(__fmul_rn(r.d.x, qvx), __fmul_rn(r.d.y, qvy)), __fmul_rn(r.d.z, qvz));
+    float T = __fadd_rn(__fadd_rn(__fmul_rn(c.x, qvx), __fmul_rn(c.y, qvy)), __fmul_rn(c.z, qvz));
+    if (det < 0.0f) {
+        det = -det;
+        U = -U;
+        Vv = -Vv;
+        T = -T;
+    }
+    if (det > 0.0f) {
+        const float eps = det * 1e-30f;
+        if (U < -eps || Vv < -eps || T < -eps) return false;
+        if (__fadd_rn(U, Vv) > det * 1.000001f) return false;
+        if (T > (det * tmax) * 1.000001f) return false;
+    }
     u = __fdiv_rn(U, det);
     v = __fdiv_rn(Vv, det);
     tt = __fdiv_rn(T, det);
     w = __fsub_rn(__fsub_rn(1.0f, u), v);
-    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f;
+    prim = __float_as_int(a.w);
+    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < tmax;
 }
-
-struct TriHit {
-    float t, u, v, w;
-    int prim, inst, mat;
-};
 
 // GLSL mat4 * vec4 with the sum in column order, no contraction
 // (closest_hit.glsl:163-164 with a precomputed inverse).
@@ -139,108 +170,149 @@ __device__ __forceinline__ V3 xform_point(const float4* __restrict__ xf, int ins
 
 __device__ __forceinline__ void flag_status(int* status, int code) { atomicCAS(status, PT_OK, code); }
 
-// One level of closest-hit traversal from wide node `root`.  For the TLAS
-// (IS_TLAS) the leaf primitives are instances, each traversed as a nested
-// BLAS level above the current stack top.
-template <bool IS_TLAS>
-__device__ __noinline__ void traverse_closest(const Params& P, int root, const TRay& r, TriHit& h, uint2* stack,
-                                              int sp, int inst, int mat) {
-    uint32_t cb, pb, im;
-    uint32_t hm = intersect_node(P.nodes, root, r, h.t, cb, pb, im);
-    uint2 ng = make_uint2(cb, (hm & 0xff000000u) | im);
-    uint32_t tbase = pb, tbits = hm & 0x00ffffffu;
-    const int sp_base = sp;
-    for (;;) {
-        while (tbits) {
-            const int b = __ffs(tbits) - 1;
-            tbits &= tbits - 1;
-            if (IS_TLAS) {
-                const int4 ir = __ldg(P.insts + tbase + b);
-                const TRay ro = ir.w ? r : prep_ray(xform_point(P.xf, ir.y, r.o, 1.0f), xform_point(P.xf, ir.y, r.d, 0.0f));
-                traverse_closest<false>(P, ir.x, ro, h, stack, sp, ir.y, ir.z);
-            } else {
-                float u, v, t, w;
-                int prim;
-                if (tri_test(r, P.tris, tbase + b, u, v, t, w, prim) && t < h.t) {
-                    h.t = t; h.u = u; h.v = v; h.w = w;
-                    h.prim = prim; h.inst = inst; h.mat = mat;
+// --------------------------------------------------------- state machine
+struct Trav {
+    TRay world, cur;   // the query ray, and the ray in the current instance's space
+    float tmax;        // closest hit so far / max distance of an any-hit query
+    // result (closest hit)
+    float u, v, w;
+    int prim, inst, mat;
+    // traversal
+    uint2 ng;          // node group: child base, internal hit bits (24-31) | imask
+    uint32_t pbase, pbits;  // pending primitives: triangles (BLAS) or instances (TLAS)
+    int next;          // node to intersect next (-1: none)
+    int sp;
+    bool blas;
+    int blas_sp, cur_inst, cur_mat;
+    uint2 tlas_ng;     // TLAS state kept while a BLAS is traversed
+    uint32_t tlas_pbase, tlas_pbits;
+};
+
+__device__ __forceinline__ void trav_init(Trav& s, const Params& P, V3 o, V3 d, float tmax) {
+    s.world = prep_ray(o, d);
+    s.cur = s.world;
+    s.tmax = tmax;
+    s.prim = -1;
+    s.inst = -1;
+    s.mat = 0;
+    s.u = s.v = s.w = 0.0f;
+    s.ng = make_uint2(0, 0);
+    s.pbase = 0;
+    s.pbits = 0;
+    s.next = P.tlas_root;
+    s.sp = 0;
+    s.blas = false;
+    s.blas_sp = 0;
+    s.cur_inst = -1;
+    s.cur_mat = 0;
+}
+
+enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };
+
+// One step.  ANY: stop at the first accepted triangle (any-hit query);
+// ALPHA (with ANY): anyhit.glsl:118-141's alpha test, drawing from rng.
+template <bool ANY, bool ALPHA>
+__device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng) {
+    if (s.pbits) {
+        const int b = __ffs(s.pbits) - 1;
+        s.pbits &= s.pbits - 1;
+        if (s.blas) {
+            float u, v, t, w;
+            int prim;
+            if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim)) {
+                if (ANY) {
+                    if (!ALPHA) return TRAV_HIT;
+                    const float4 ap = __ldg(P.mats + 8 * s.cur_mat + 7);  // opacity, alphaMode, cutoff
+                    const int alphaMode = (int)ap.y;
+                    bool skip = alphaMode == ALPHA_MODE_MASK && ap.x < ap.z;
+                    if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > ap.x;
+                    if (!skip) return TRAV_HIT;
+                } else {
+                    s.tmax = t;
+                    s.u = u; s.v = v; s.w = w;
+                    s.prim = prim;
+                    s.inst = s.cur_inst;
+                    s.mat = s.cur_mat;
                 }
             }
-        }
-        if (ng.y > 0x00ffffffu) {
-            const uint32_t bit = 31u - __clz(ng.y);
-            const uint32_t slot = (bit - 24u) ^ r.oct_inv;
-            const uint32_t rel = __popc(ng.y & ~(0xffffffffu << slot));
-            const int child = (int)(ng.x + rel);
-            ng.y &= ~(1u << bit);
-            if (ng.y > 0x00ffffffu) {
-                if (sp < kStackSize) stack[sp++] = ng;
-                else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
-            }
-            hm = intersect_node(P.nodes, child, r, h.t, cb, pb, im);
-            ng = make_uint2(cb, (hm & 0xff000000u) | im);
-            tbase = pb;
-            tbits = hm & 0x00ffffffu;
         } else {
-            if (sp == sp_base) break;
-            ng = stack[--sp];
+            // enter instance: keep the TLAS position, traverse its BLAS
+            const int4 ir = __ldg(P.insts + s.pbase + b);
+            s.tlas_ng = s.ng;
+            s.tlas_pbase = s.pbase;
+            s.tlas_pbits = s.pbits;
+            s.pbits = 0;
+            s.ng = make_uint2(0, 0);
+            s.blas = true;
+            s.blas_sp = s.sp;
+            s.cur_inst = ir.y;
+            s.cur_mat = ir.z;
+            s.cur = ir.w ? s.world
+                         : prep_ray(xform_point(P.xf, ir.y, s.world.o, 1.0f), xform_point(P.xf, ir.y, s.world.d, 0.0f));
+            s.next = ir.x;
         }
+        return TRAV_RUNNING;
+    }
+    if (s.next < 0 && s.ng.y > 0x00ffffffu) {
+        const uint32_t bit = 31u - __clz(s.ng.y);
+        const uint32_t slot = (bit - 24u) ^ s.cur.oct_inv;
+        const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << slot));
+        s.next = (int)(s.ng.x + rel);
+        s.ng.y &= ~(1u << bit);
+        if (s.ng.y > 0x00ffffffu) {
+            if (s.sp < kStackSize) stack[s.sp++] = s.ng;
+            else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
+        }
+    }
+    if (s.next >= 0) {
+        uint32_t cb, pb, im;
+        const uint32_t hm = intersect_node(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
+        s.next = -1;
+        s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
+        s.pbase = pb;
+        s.pbits = hm & 0x00ffffffu;
+        return TRAV_RUNNING;
+    }
+    // the current group is exhausted
+    if (s.sp > (s.blas ? s.blas_sp : 0)) {
+        s.ng = stack[--s.sp];
+        return TRAV_RUNNING;
+    }
+    if (s.blas) {  // back to the TLAS
+        s.blas = false;
+        s.cur = s.world;
+        s.ng = s.tlas_ng;
+        s.pbase = s.tlas_pbase;
+        s.pbits = s.tlas_pbits;
+        return TRAV_RUNNING;
+    }
+    return TRAV_DONE;
+}
+
+// Closest triangle hit along (o, d) closer than tmax: fills s.prim (-1 if
+// none), s.tmax, barycentrics, instance and material.
+__device__ __forceinline__ void trace_closest(Trav& s, const Params& P, V3 o, V3 d, float tmax, uint2* stack) {
+    trav_init(s, P, o, d, tmax);
+    while (trav_step<false, false>(s, P, stack, nullptr) == TRAV_RUNNING) {
     }
 }
 
-// Any-hit traversal (anyhit.glsl:83-213): true as soon as a triangle with
-// 0 <= t < maxDist passes the (optional) alpha test.
-template <bool IS_TLAS>
-__device__ __noinline__ bool traverse_any(const Params& P, int root, const TRay& r, float maxDist, uint2* stack,
-                                          int sp, int mat, bool alpha, Rng& rng) {
-    uint32_t cb, pb, im;
-    uint32_t hm = intersect_node(P.nodes, root, r, maxDist, cb, pb, im);
-    uint2 ng = make_uint2(cb, (hm & 0xff000000u) | im);
-    uint32_t tbase = pb, tbits = hm & 0x00ffffffu;
-    const int sp_base = sp;
-    for (;;) {
-        while (tbits) {
-            const int b = __ffs(tbits) - 1;
-            tbits &= tbits - 1;
-            if (IS_TLAS) {
-                const int4 ir = __ldg(P.insts + tbase + b);
-                const TRay ro = ir.w ? r : prep_ray(xform_point(P.xf, ir.y, r.o, 1.0f), xform_point(P.xf, ir.y, r.d, 0.0f));
-                if (traverse_any<false>(P, ir.x, ro, maxDist, stack, sp, ir.z, alpha, rng)) return true;
-            } else {
-                float u, v, t, w;
-                int prim;
-                if (tri_test(r, P.tris, tbase + b, u, v, t, w, prim) && t < maxDist) {
-                    if (!alpha) return true;
-                    // anyhit.glsl:118-141 with no texture bound (alpha = 1)
-                    const float4 ap = __ldg(P.mats + 8 * mat + 7);
-                    const float opacity = ap.x;
-                    const int alphaMode = (int)ap.y;
-                    bool skip = alphaMode == ALPHA_MODE_MASK && opacity < ap.z;
-                    if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng.next() > opacity;
-                    if (!skip) return true;
-                }
-            }
-        }
-        if (ng.y > 0x00ffffffu) {
-            const uint32_t bit = 31u - __clz(ng.y);
-            const uint32_t slot = (bit - 24u) ^ r.oct_inv;
-            const uint32_t rel = __popc(ng.y & ~(0xffffffffu << slot));
-            const int child = (int)(ng.x + rel);
-            ng.y &= ~(1u << bit);
-            if (ng.y > 0x00ffffffu) {
-                if (sp < kStackSize) stack[sp++] = ng;
-                else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
-            }
-            hm = intersect_node(P.nodes, child, r, maxDist, cb, pb, im);
-            ng = make_uint2(cb, (hm & 0xff000000u) | im);
-            tbase = pb;
-            tbits = hm & 0x00ffffffu;
-        } else {
-            if (sp == sp_base) break;
-            ng = stack[--sp];
+// True if a triangle lies at 0 <= t < maxDist (and passes the alpha test
+// when `alpha`).
+static __device__ __noinline__ bool trace_any(const Params& P, V3 o, V3 d, float maxDist, bool alpha, Rng& rng,
+                                              uint2* stack) {
+    Trav s;
+    trav_init(s, P, o, d, maxDist);
+    if (alpha) {
+        for (;;) {
+            const int st = trav_step<true, true>(s, P, stack, &rng);
+            if (st != TRAV_RUNNING) return st == TRAV_HIT;
         }
     }
-    return false;
+    for (;;) {
+        const int st = trav_step<true, false>(s, P, stack, nullptr);
+        if (st != TRAV_RUNNING) return st == TRAV_HIT;
+    }
 }
 
 }  // namespace ptgb

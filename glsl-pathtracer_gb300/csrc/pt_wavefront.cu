@@ -36,7 +36,7 @@ struct WfView {  // device pointers of WavefrontBuffers, by value
     float4* rad;
     int* q[2];
     int* qs;
-    int* counts;  // [0], [1] extension queues, [2] shadow queue
+    int* counts;  // [0], [1] extension queues, [2] shadow queue, [4], [5] fetch counters of extend / shadow
 };
 
 __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps) {
@@ -101,28 +101,61 @@ __global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfVie
         B.counts[0] = n;
         B.counts[1] = 0;
         B.counts[2] = 0;
+        B.counts[4] = 0;  // fetch counters of the extend and shadow stages
+        B.counts[5] = 0;
     }
     add_counters(P, 0, 0, paths);
 }
 
+// Each thread of a warp that has no ray takes the next one from the queue
+// (one atomic per warp); returns the queue slot or -1.
+__device__ __forceinline__ int fetch_work(int* counter, int n, bool need) {
+    const int lane = threadIdx.x & 31;
+    const unsigned needm = __ballot_sync(0xffffffffu, need);
+    if (!needm) return -1;
+    const int leader = __ffs(needm) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(needm));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!need) return -1;
+    const int k = base + __popc(needm & ((1u << lane) - 1));
+    return k < n ? k : -1;
+}
+
+// Closest-hit queries of the queue.  Persistent: a thread whose ray is done
+// fetches the next one while the rest of its warp keeps traversing, so the
+// warp's lanes stay busy however unequal the rays are.
 __global__ void __launch_bounds__(128) wf_extend(Params P, WfView B, int in) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         B.counts[in ^ 1] = 0;  // the next queue and the shadow queue start empty
         B.counts[2] = 0;
+        B.counts[5] = 0;       // fetch counter of the shadow stage
     }
     Counters cnt{0, 0};
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const int i = B.q[in][j];
-        const float4 o = B.o[i], d = B.d[i];
-        const int depth = B.misc[i].x;
-        const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
-        HitRecord hr;
-        TraceClosest(P, r, depth, hr, stack, cnt, false);
-        B.h0[i] = make_float4(hr.t, hr.u, hr.v, hr.w);
-        B.h1[i] = make_int4(hr.prim, hr.inst, hr.mat, (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 : 0));
-        B.h2[i] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
+    Trav s;
+    HitRecord hr;
+    float tl = PT_INF;
+    int ray = -1;
+    for (;;) {
+        const int k = fetch_work(B.counts + 4, n, ray < 0);
+        if (k >= 0) {
+            ray = B.q[in][k];
+            const float4 o = B.o[ray], d = B.d[ray];
+            const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
+            tl = LightsClosest(P, r, B.misc[ray].x, hr);
+            trav_init(s, P, r.origin, r.direction, tl);
+            cnt.closest++;
+        }
+        if (!__any_sync(0xffffffffu, ray >= 0)) break;
+        if (ray >= 0 && trav_step<false, false>(s, P, stack, nullptr) != TRAV_RUNNING) {
+            FinishClosest(s, tl, hr);
+            B.h0[ray] = make_float4(hr.t, hr.u, hr.v, hr.w);
+            B.h1[ray] = make_int4(hr.prim, hr.inst, hr.mat, (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 : 0));
+            B.h2[ray] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
+            ray = -1;
+        }
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
@@ -180,33 +213,73 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
 
+// Any-hit queries of the shadow queue (one or two rays per path: the env
+// sample first, then the light sample), persistent like wf_extend.  The
+// deferred form is used only when AnyHit draws no random numbers.
 __global__ void __launch_bounds__(128) wf_shadow(Params P, WfView B) {
     uint2 stack[kStackSize];
     const int n = B.counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
     Counters cnt{0, 0};
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const int i = B.qs[j];
-        const float4 so = B.so[i];
-        const int bits = __float_as_int(so.w);
+    Trav s;
+    // per-thread stage: 0 start env ray, 1 tracing it, 2 start light ray,
+    // 3 tracing it, 4 both resolved
+    int path = -1, bits = 0, stage = 0;
+    bool occ0 = false, occ1 = false;
+    V3 origin = v3(0.0f);
+    for (;;) {
+        const int k = fetch_work(B.counts + 5, n, path < 0);
+        if (k >= 0) {
+            path = B.qs[k];
+            const float4 so = B.so[path];
+            bits = __float_as_int(so.w);
+            origin = v3(so.x, so.y, so.z);
+            occ0 = occ1 = false;
+            stage = 0;
+        }
+        if (!__any_sync(0xffffffffu, path >= 0)) break;
+        if (path < 0) continue;
+        if (stage == 0 || stage == 2) {
+            const int which = stage >> 1;
+            if (bits & (1 << which)) {
+                const float4 d = which ? B.sd1[path] : B.sd0[path];
+                const Ray r{origin, v3(d.x, d.y, d.z)};
+                cnt.shadow++;
+                if (LightsAny(P, r, d.w)) {
+                    if (which) occ1 = true;
+                    else occ0 = true;
+                    stage += 2;
+                } else {
+                    trav_init(s, P, r.origin, r.direction, d.w);
+                    stage += 1;
+                }
+            } else {
+                stage += 2;
+            }
+        }
+        if (stage == 1 || stage == 3) {
+            const int st = trav_step<true, false>(s, P, stack, nullptr);
+            if (st != TRAV_RUNNING) {
+                if (stage == 1) occ0 = st == TRAV_HIT;
+                else occ1 = st == TRAV_HIT;
+                stage += 1;
+            }
+        }
+        if (stage != 4) continue;
+        // both rays resolved: radiance += Ld * T
         ShadowReq sr;
         sr.n = bits & 3;
         sr.adds = (bits >> 2) & 3;
-        const V3 origin = v3(so.x, so.y, so.z);
-        Rng rng;  // the deferred form is used only when AnyHit draws no random numbers
-        rng.x = rng.y = rng.z = rng.w = 0;
-        bool occ0 = false, occ1 = false;
         if (sr.n & 1) {
-            const float4 d = B.sd0[i];
-            const float4 c = B.sc0[i];
+            const float4 c = B.sc0[path];
             sr.contrib[0] = v3(c.x, c.y, c.z);
-            occ0 = AnyHit(P, Ray{origin, v3(d.x, d.y, d.z)}, d.w, rng, stack, cnt);
         }
         if (sr.n & 2) {
-            const float4 d = B.sd1[i];
-            const float4 c = B.sc1[i];
+            const float4 c = B.sc1[path];
             sr.contrib[1] = v3(c.x, c.y, c.z);
-            occ1 = AnyHit(P, Ray{origin, v3(d.x, d.y, d.z)}, d.w, rng, stack, cnt);
         }
+        const int i = path;
+        path = -1;
         const float4 T = B.sT[i];
         const V3 Ld = ResolveShadow(sr, occ0, occ1);
         float4 L = B.L[i];
@@ -297,7 +370,7 @@ cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity) {
         (e = cudaMalloc((void**)&wb.q[0], n * sizeof(int))) != cudaSuccess ||
         (e = cudaMalloc((void**)&wb.q[1], n * sizeof(int))) != cudaSuccess ||
         (e = cudaMalloc((void**)&wb.qs, n * sizeof(int))) != cudaSuccess ||
-        (e = cudaMalloc((void**)&wb.counts, 4 * sizeof(int))) != cudaSuccess) {
+        (e = cudaMalloc((void**)&wb.counts, 8 * sizeof(int))) != cudaSuccess) {
         wavefront_free(wb);
         return e;
     }
