@@ -113,7 +113,7 @@ __device__ __forceinline__ void FinishClosest(const Trav& s, float tLight, HitRe
     hr.mat = s.mat;
     hr.u = s.u;
     hr.v = s.v;
-    hr.w = s.w;
+    hr.w = __fsub_rn(__fsub_rn(1.0f, s.u), s.v);  // uvt.w, as the triangle test computed it
 }
 
 __device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int depth, HitRecord& hr, uint2* stack,

@@ -10,9 +10,9 @@
 // so that the threads of a warp stay in one loop whatever level and stage
 // each ray is at, and a thread whose ray finished can take a new one at once
 // (the persistent kernels of pt_wavefront.cu).  Both levels of the
-// reference's two-level BVH run in the same loop: entering an instance keeps
-// the TLAS node group and the remaining instance bits in registers and marks
-// the stack height; leaving the BLAS restores them.
+// reference's two-level BVH run in the same loop: entering an instance
+// pushes the TLAS node group, the remaining instance bits and a sentinel;
+// popping the sentinel restores them and leaves the BLAS.
 //
 // The triangle test repeats the reference's arithmetic operation for
 // operation, without fused multiply-adds (closest_hit.glsl:128-143), so hit
@@ -30,11 +30,12 @@
 
 namespace ptgb {
 
+// A ray prepared for slab tests: 1/d and the inverse octant (7 - octant of
+// d; bit k clear when d points towards -k).
 struct TRay {
     V3 o, d;
     float ix, iy, iz;
-    uint32_t oct_inv, oct_inv4;
-    bool nx, ny, nz;
+    uint32_t oct_inv;
 };
 
 __device__ __forceinline__ float safe_rcp(float d) {
@@ -48,14 +49,12 @@ __device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
     r.ix = safe_rcp(d.x);
     r.iy = safe_rcp(d.y);
     r.iz = safe_rcp(d.z);
-    r.nx = r.ix < 0.0f;
-    r.ny = r.iy < 0.0f;
-    r.nz = r.iz < 0.0f;
-    const uint32_t oct = (r.nx ? 1u : 0u) | (r.ny ? 2u : 0u) | (r.nz ? 4u : 0u);
+    const uint32_t oct = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
     r.oct_inv = 7u - oct;
-    r.oct_inv4 = r.oct_inv * 0x01010101u;
     return r;
 }
+
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
 // Byte j of w as a float, without the (quarter-rate) integer conversion:
 // the byte becomes the low mantissa bits of 2^23, which is then subtracted.
@@ -79,19 +78,21 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
     const float orgx = (__uint_as_float(w0.x) - r.o.x) * r.ix;
     const float orgy = (__uint_as_float(w0.y) - r.o.y) * r.iy;
     const float orgz = (__uint_as_float(w0.z) - r.o.z) * r.iz;
+    const uint32_t oct_inv4 = r.oct_inv * 0x01010101u;
+    const bool nx = !(r.oct_inv & 1u), ny = !(r.oct_inv & 2u), nz = !(r.oct_inv & 4u);
     uint32_t hits = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         const uint32_t meta4 = half ? w1.w : w1.z;
         const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
         const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xffu;
-        const uint32_t bit_index4 = (meta4 ^ (r.oct_inv4 & inner_mask4)) & 0x1f1f1f1fu;
+        const uint32_t bit_index4 = (meta4 ^ (oct_inv4 & inner_mask4)) & 0x1f1f1f1fu;
         const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
         const uint32_t qlox = half ? w2.y : w2.x, qloy = half ? w2.w : w2.z, qloz = half ? w3.y : w3.x;
         const uint32_t qhix = half ? w3.w : w3.z, qhiy = half ? w4.y : w4.x, qhiz = half ? w4.w : w4.z;
-        const uint32_t nxw = r.nx ? qhix : qlox, fxw = r.nx ? qlox : qhix;
-        const uint32_t nyw = r.ny ? qhiy : qloy, fyw = r.ny ? qloy : qhiy;
-        const uint32_t nzw = r.nz ? qhiz : qloz, fzw = r.nz ? qloz : qhiz;
+        const uint32_t nxw = nx ? qhix : qlox, fxw = nx ? qlox : qhix;
+        const uint32_t nyw = ny ? qhiy : qloy, fyw = ny ? qloy : qhiy;
+        const uint32_t nzw = nz ? qhiz : qloz, fzw = nz ? qloz : qhiz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const float tnx = fmaf(qbyte(nxw, j), adjx, orgx), tfx = fmaf(qbyte(fxw, j), adjx, orgx);
@@ -171,52 +172,58 @@ __device__ __forceinline__ V3 xform_point(const float4* __restrict__ xf, int ins
 __device__ __forceinline__ void flag_status(int* status, int code) { atomicCAS(status, PT_OK, code); }
 
 // --------------------------------------------------------- state machine
+// Entering an instance pushes the TLAS position (node group, then pending
+// instances) and a sentinel; popping the sentinel leaves the BLAS.
+constexpr uint32_t kBlasSentinel = 0xffffffffu;
+
 struct Trav {
-    TRay world, cur;   // the query ray, and the ray in the current instance's space
+    V3 wo, wd;         // the query ray (world space)
+    TRay cur;          // the ray in the current instance's space
     float tmax;        // closest hit so far / max distance of an any-hit query
-    // result (closest hit)
-    float u, v, w;
+    float u, v;        // result (closest hit)
     int prim, inst, mat;
-    // traversal
     uint2 ng;          // node group: child base, internal hit bits (24-31) | imask
     uint32_t pbase, pbits;  // pending primitives: triangles (BLAS) or instances (TLAS)
     int next;          // node to intersect next (-1: none)
     int sp;
-    bool blas;
-    int blas_sp, cur_inst, cur_mat;
-    uint2 tlas_ng;     // TLAS state kept while a BLAS is traversed
-    uint32_t tlas_pbase, tlas_pbits;
+    int cur_inst, cur_mat;  // instance being traversed (-1: the TLAS)
 };
 
 __device__ __forceinline__ void trav_init(Trav& s, const Params& P, V3 o, V3 d, float tmax) {
-    s.world = prep_ray(o, d);
-    s.cur = s.world;
+    s.wo = o;
+    s.wd = d;
+    s.cur = prep_ray(o, d);
     s.tmax = tmax;
     s.prim = -1;
     s.inst = -1;
     s.mat = 0;
-    s.u = s.v = s.w = 0.0f;
+    s.u = s.v = 0.0f;
     s.ng = make_uint2(0, 0);
     s.pbase = 0;
     s.pbits = 0;
     s.next = P.tlas_root;
     s.sp = 0;
-    s.blas = false;
-    s.blas_sp = 0;
     s.cur_inst = -1;
     s.cur_mat = 0;
 }
 
 enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };
 
+__device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp, uint2 e) {
+    if (sp < kStackSize) stack[sp++] = e;
+    else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
+}
+
 // One step.  ANY: stop at the first accepted triangle (any-hit query);
 // ALPHA (with ANY): anyhit.glsl:118-141's alpha test, drawing from rng.
 template <bool ANY, bool ALPHA>
 __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng) {
+    const bool in_blas = s.cur_inst >= 0;
     if (s.pbits) {
         const int b = __ffs(s.pbits) - 1;
         s.pbits &= s.pbits - 1;
-        if (s.blas) {
+        if (in_blas) {
+            if (s.pbits) prefetch_l1(P.tris + 3 * (size_t)(s.pbase + __ffs(s.pbits) - 1));
             float u, v, t, w;
             int prim;
             if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim)) {
@@ -229,26 +236,25 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                     if (!skip) return TRAV_HIT;
                 } else {
                     s.tmax = t;
-                    s.u = u; s.v = v; s.w = w;
+                    s.u = u;
+                    s.v = v;
                     s.prim = prim;
                     s.inst = s.cur_inst;
                     s.mat = s.cur_mat;
                 }
             }
         } else {
-            // enter instance: keep the TLAS position, traverse its BLAS
+            // enter an instance: park the TLAS position on the stack
             const int4 ir = __ldg(P.insts + s.pbase + b);
-            s.tlas_ng = s.ng;
-            s.tlas_pbase = s.pbase;
-            s.tlas_pbits = s.pbits;
+            trav_push(P, stack, s.sp, s.ng);
+            trav_push(P, stack, s.sp, make_uint2(s.pbase, s.pbits));
+            trav_push(P, stack, s.sp, make_uint2(kBlasSentinel, 0u));
             s.pbits = 0;
             s.ng = make_uint2(0, 0);
-            s.blas = true;
-            s.blas_sp = s.sp;
             s.cur_inst = ir.y;
             s.cur_mat = ir.z;
-            s.cur = ir.w ? s.world
-                         : prep_ray(xform_point(P.xf, ir.y, s.world.o, 1.0f), xform_point(P.xf, ir.y, s.world.d, 0.0f));
+            s.cur = ir.w ? prep_ray(s.wo, s.wd)
+                         : prep_ray(xform_point(P.xf, ir.y, s.wo, 1.0f), xform_point(P.xf, ir.y, s.wd, 0.0f));
             s.next = ir.x;
         }
         return TRAV_RUNNING;
@@ -259,10 +265,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << slot));
         s.next = (int)(s.ng.x + rel);
         s.ng.y &= ~(1u << bit);
-        if (s.ng.y > 0x00ffffffu) {
-            if (s.sp < kStackSize) stack[s.sp++] = s.ng;
-            else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
-        }
+        if (s.ng.y > 0x00ffffffu) trav_push(P, stack, s.sp, s.ng);
     }
     if (s.next >= 0) {
         uint32_t cb, pb, im;
@@ -271,19 +274,30 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
         s.pbase = pb;
         s.pbits = hm & 0x00ffffffu;
+        if (s.pbits) {  // the next step tests a triangle (or enters an instance)
+            if (in_blas) prefetch_l1(P.tris + 3 * (size_t)(pb + __ffs(s.pbits) - 1));
+        } else if (s.ng.y > 0x00ffffffu) {  // or intersects the nearest child
+            const uint32_t bit = 31u - __clz(s.ng.y);
+            const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << ((bit - 24u) ^ s.cur.oct_inv)));
+            const char* np = reinterpret_cast<const char*>(P.nodes + (size_t)(cb + rel) * 5);
+            prefetch_l1(np);
+            prefetch_l1(np + 64);
+        }
         return TRAV_RUNNING;
     }
-    // the current group is exhausted
-    if (s.sp > (s.blas ? s.blas_sp : 0)) {
-        s.ng = stack[--s.sp];
-        return TRAV_RUNNING;
-    }
-    if (s.blas) {  // back to the TLAS
-        s.blas = false;
-        s.cur = s.world;
-        s.ng = s.tlas_ng;
-        s.pbase = s.tlas_pbase;
-        s.pbits = s.tlas_pbits;
+    // the current group is exhausted: pop
+    if (s.sp > 0) {
+        const uint2 e = stack[--s.sp];
+        if (e.x == kBlasSentinel) {  // back to the TLAS
+            const uint2 pend = stack[--s.sp];
+            s.ng = stack[--s.sp];
+            s.pbase = pend.x;
+            s.pbits = pend.y;
+            s.cur_inst = -1;
+            s.cur = prep_ray(s.wo, s.wd);
+        } else {
+            s.ng = e;
+        }
         return TRAV_RUNNING;
     }
     return TRAV_DONE;

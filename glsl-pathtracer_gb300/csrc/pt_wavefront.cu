@@ -125,7 +125,9 @@ __device__ __forceinline__ int fetch_work(int* counter, int n, bool need) {
 // Closest-hit queries of the queue.  Persistent: a thread whose ray is done
 // fetches the next one while the rest of its warp keeps traversing, so the
 // warp's lanes stay busy however unequal the rays are.
-__global__ void __launch_bounds__(128) wf_extend(Params P, WfView B, int in) {
+// Traversal is memory-latency bound: 8 blocks of 128 threads (64 registers)
+// keep 32 warps per SM in flight.
+__global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
 // Any-hit queries of the shadow queue (one or two rays per path: the env
 // sample first, then the light sample), persistent like wf_extend.  The
 // deferred form is used only when AnyHit draws no random numbers.
-__global__ void __launch_bounds__(128) wf_shadow(Params P, WfView B) {
+__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B) {
     uint2 stack[kStackSize];
     const int n = B.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
