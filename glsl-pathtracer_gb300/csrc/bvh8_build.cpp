@@ -6,10 +6,19 @@
 // pre-order binary nodes with LRLeaf = (left, right, 0) for interior nodes,
 // (firstTri, numTris, 1) for BLAS leaves and (blasRoot, materialID,
 // -instance-1) for TLAS leaves, BLASes first and the TLAS from
-// topLevelIndex on.  The wide tree keeps the binary tree's boxes: each wide
-// node takes up to eight binary descendants, chosen greedily by expanding the
-// interior child of largest surface area (so the wide tree visits the same
-// triangles the binary one does, with fewer, larger node fetches).
+// topLevelIndex on.  Each wide node takes up to eight binary descendants,
+// chosen greedily by expanding the interior child of largest surface area,
+// so the wide tree holds the binary tree's boxes with fewer, larger nodes.
+//
+// Instances whose transform is the identity are merged: their triangles get
+// one BLAS of their own (binned SAH, sah_builder.h), each triangle carrying
+// its instance and material in the spare lanes of its WideTri record, and
+// the TLAS is rebuilt over that BLAS and the remaining instances.  The
+// reference gives every mesh its own instance (one material per instance),
+// so scenes made of many untransformed meshes would otherwise pay for
+// overlapping instance boxes on every ray.  Hits (triangle, instance,
+// material, distance) are unchanged: the same triangles are tested with the
+// same arithmetic in the same space.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -20,6 +29,7 @@
 
 #include "../../include/pt_cuda.h"
 #include "bvh8.h"
+#include "sah_builder.h"
 
 using namespace ptgb;
 
@@ -27,7 +37,7 @@ namespace {
 
 struct BinNode {
     float lo[3], hi[3];
-    int l, r, leaf;
+    int l, r, leaf;  // leaf: 0 interior, 1 BLAS leaf, 2 merged leaf (range of Impl::merged), <0 TLAS leaf
 };
 
 struct Box {
@@ -47,31 +57,41 @@ struct Box {
 };
 
 // A child candidate of a wide node: a binary interior node, or a primitive
-// range [first, first+count) (triangles in a BLAS, one instance in the TLAS).
+// range [first, first+count) (triangles in a BLAS, entries of the merged
+// triangle list, or one instance in the TLAS).
 struct Child {
     int bin = -1;        // binary interior node index (range children: -1)
     int first = 0, count = 0;
+    bool merged = false;
     int blas_root = -1, material = 0;  // TLAS leaf data
     Box box;
     bool is_range() const { return bin < 0; }
     bool is_leaf_slot() const { return bin < 0 && count <= 3; }
 };
 
+struct MergedTri {
+    int tri, inst, mat;
+};
+
+constexpr int kMergedInstance = 0x7fffffff;  // InstRef.instance of the merged BLAS
+
 struct Impl {
+    // inputs (copies, so instance updates can rebuild)
     std::vector<BinNode> bn;
+    int top = 0;
+    std::vector<int32_t> vidx;
+    std::vector<float> verts;  // xyz per vertex
+    int num_tris = 0, num_vertices = 0, num_instances = 0;
+    std::vector<float> transforms;
+    // outputs
     std::vector<WideNode> nodes;
     std::vector<WideTri> tris;
     std::vector<InstRef> insts;
     std::vector<int> inst_identity;
+    std::vector<MergedTri> merged;
     std::map<int, int> blas_root_map;  // binary BLAS root -> wide node index
-    int blas_node_count = 0;
-    int blas_tri_count = 0;
-    const int32_t* vidx = nullptr;
-    const float* verts = nullptr;
-    int num_tris = 0, num_vertices = 0, num_instances = 0;
     bool tlas = false;
     int max_depth = 0;
-    std::string err;
 };
 
 struct BuildError {
@@ -80,22 +100,24 @@ struct BuildError {
 
 [[noreturn]] void fail(const std::string& m) { throw BuildError{m}; }
 
-Box tri_box(Impl& I, int t) {
+int tri_of(const Impl& I, int k, bool merged) { return merged ? I.merged[k].tri : k; }
+
+Box tri_box(const Impl& I, int t) {
     if (t < 0 || t >= I.num_tris) fail("leaf triangle index out of range: " + std::to_string(t));
     Box b;
     b.empty();
     for (int k = 0; k < 3; ++k) {
         int v = I.vidx[3 * (size_t)t + k];
         if (v < 0 || v >= I.num_vertices) fail("vertex index out of range: " + std::to_string(v));
-        b.grow(I.verts + 4 * (size_t)v);
+        b.grow(&I.verts[3 * (size_t)v]);
     }
     return b;
 }
 
-Box range_box(Impl& I, int first, int count) {
+Box range_box(const Impl& I, int first, int count, bool merged) {
     Box b;
     b.empty();
-    for (int i = 0; i < count; ++i) b.grow(tri_box(I, first + i));
+    for (int i = 0; i < count; ++i) b.grow(tri_box(I, tri_of(I, first + i, merged)));
     return b;
 }
 
@@ -105,8 +127,8 @@ Box node_box(const BinNode& n) {
     return b;
 }
 
-// Children contributed by binary node `b` (one entry, or leaf ranges).
-void children_of(Impl& I, int b, std::vector<Child>& out) {
+// Children contributed by binary node `b` (one entry, or a leaf range).
+void children_of(const Impl& I, int b, std::vector<Child>& out) {
     if (b < 0 || b >= (int)I.bn.size()) fail("child node index out of range: " + std::to_string(b));
     const BinNode& n = I.bn[b];
     Child c;
@@ -120,18 +142,17 @@ void children_of(Impl& I, int b, std::vector<Child>& out) {
         if (n.r == 0) return;
         c.first = n.l;
         c.count = n.r;
-        // a reference leaf holds < 4 triangles and its box bounds them; bigger
-        // leaves are split into ranges later, with boxes from the triangles
-        c.box = n.r <= 3 ? node_box(n) : range_box(I, n.l, n.r);
-        if (n.r <= 3) {
-            Box tb = range_box(I, n.l, n.r);  // validates indices
-            (void)tb;
-        }
+        c.merged = n.leaf == 2;
+        if (c.merged && (n.l < 0 || n.l + n.r > (int)I.merged.size())) fail("merged leaf out of range");
+        // a reference leaf holds < 4 triangles and its box bounds them; the
+        // triangles' own box is used for bigger ones (they are split later)
+        Box tb = range_box(I, c.first, c.count, c.merged);  // also validates the indices
+        c.box = n.r <= 3 ? node_box(n) : tb;
         out.push_back(c);
     } else {
         if (!I.tlas) fail("TLAS leaf reached inside a BLAS (node " + std::to_string(b) + ")");
         int inst = -n.leaf - 1;
-        if (inst >= I.num_instances) fail("instance index out of range: " + std::to_string(inst));
+        if (inst >= I.num_instances && inst != kMergedInstance) fail("instance index out of range: " + std::to_string(inst));
         c.first = inst;
         c.count = 1;
         c.blas_root = n.l;
@@ -142,14 +163,15 @@ void children_of(Impl& I, int b, std::vector<Child>& out) {
 }
 
 // Split a primitive range of more than 3 primitives into up to 8 pieces.
-void split_range(Impl& I, const Child& c, std::vector<Child>& out) {
+void split_range(const Impl& I, const Child& c, std::vector<Child>& out) {
     int pieces = std::min(8, (c.count + 2) / 3);
     int per = (c.count + pieces - 1) / pieces;
     for (int f = c.first; f < c.first + c.count; f += per) {
         Child r;
         r.first = f;
         r.count = std::min(per, c.first + c.count - f);
-        r.box = range_box(I, r.first, r.count);
+        r.merged = c.merged;
+        r.box = range_box(I, r.first, r.count, r.merged);
         out.push_back(r);
     }
 }
@@ -300,21 +322,28 @@ void build_node(Impl& I, const std::vector<Child>& initial, int target, int dept
             r.blas_root = it->second;
             r.instance = c.first;
             r.material = c.material;
-            r.identity = I.inst_identity[c.first];
+            r.identity = c.first == kMergedInstance ? 1 : I.inst_identity[c.first];
             I.insts.push_back(r);
         } else {
-            for (int t = c.first; t < c.first + c.count; ++t) {
+            for (int k = c.first; k < c.first + c.count; ++k) {
+                const int t = tri_of(I, k, c.merged);
                 WideTri wt;
-                const int32_t* vi = I.vidx + 3 * (size_t)t;
-                const float* a = I.verts + 4 * (size_t)vi[0];
-                const float* b = I.verts + 4 * (size_t)vi[1];
-                const float* d = I.verts + 4 * (size_t)vi[2];
-                for (int k = 0; k < 3; ++k) {
-                    wt.v0[k] = a[k];
-                    wt.e0[k] = b[k] - a[k];  // the shader's e0 = v1.xyz - v0.xyz (closest_hit.glsl:128)
-                    wt.e1[k] = d[k] - a[k];  // e1 = v2.xyz - v0.xyz
+                const int32_t* vi = &I.vidx[3 * (size_t)t];
+                const float* a = &I.verts[3 * (size_t)vi[0]];
+                const float* b = &I.verts[3 * (size_t)vi[1]];
+                const float* d = &I.verts[3 * (size_t)vi[2]];
+                for (int j = 0; j < 3; ++j) {
+                    wt.v0[j] = a[j];
+                    wt.e0[j] = b[j] - a[j];  // the shader's e0 = v1.xyz - v0.xyz (closest_hit.glsl:128)
+                    wt.e1[j] = d[j] - a[j];  // e1 = v2.xyz - v0.xyz
                 }
-                wt.e0[3] = wt.e1[3] = 0.0f;
+                int inst = 0, mat = 0;
+                if (c.merged) {
+                    inst = I.merged[k].inst;
+                    mat = I.merged[k].mat;
+                }
+                std::memcpy(&wt.e0[3], &inst, 4);
+                std::memcpy(&wt.e1[3], &mat, 4);
                 wt.prim = t;
                 I.tris.push_back(wt);
             }
@@ -351,17 +380,18 @@ int build_root(Impl& I, int bin_root) {
     return target;
 }
 
-void read_binary(Impl& I, const float* nodes, int n) {
-    I.bn.resize(n);
-    for (int i = 0; i < n; ++i) {
+void read_binary(std::vector<BinNode>& bn, const float* nodes, int first, int n) {
+    for (int i = first; i < n; ++i) {
         const float* p = nodes + 9 * (size_t)i;
-        BinNode& b = I.bn[i];
+        BinNode& b = bn[i];
         for (int k = 0; k < 3; ++k) { b.lo[k] = p[k]; b.hi[k] = p[3 + k]; }
         b.l = (int)p[6]; b.r = (int)p[7]; b.leaf = (int)p[8];
+        if (b.leaf == 2) b.leaf = 1;  // only the merge step makes merged leaves
     }
 }
 
-void collect_blas_roots(Impl& I, int top, std::vector<int>& roots) {
+// TLAS leaves reachable from `top`: (node index) in tree order.
+void collect_tlas_leaves(const Impl& I, int top, std::vector<int>& leaves) {
     std::vector<int> stack{top};
     std::vector<char> seen(I.bn.size(), 0);
     while (!stack.empty()) {
@@ -373,17 +403,164 @@ void collect_blas_roots(Impl& I, int top, std::vector<int>& roots) {
         const BinNode& n = I.bn[b];
         if (n.leaf < 0) {
             if (n.l < 0 || n.l >= (int)I.bn.size()) fail("BLAS root index out of range");
-            roots.push_back(n.l);
+            leaves.push_back(b);
         } else if (n.leaf == 0) {
-            stack.push_back(n.l);
             stack.push_back(n.r);
+            stack.push_back(n.l);
         } else {
             fail("BLAS leaf inside the TLAS");
         }
     }
 }
 
-void publish(Impl& I, WideBVH* out) {
+// Triangle ranges of the BLAS rooted at `root` (binary leaves, in order).
+void collect_blas_tris(const Impl& I, int root, std::vector<int>& tris_out) {
+    std::vector<int> stack{root};
+    size_t guard = 0;
+    while (!stack.empty()) {
+        if (++guard > 4 * I.bn.size() + 16) fail("BLAS is not a tree");
+        int b = stack.back();
+        stack.pop_back();
+        if (b < 0 || b >= (int)I.bn.size()) fail("BLAS child index out of range");
+        const BinNode& n = I.bn[b];
+        if (n.leaf == 0) {
+            stack.push_back(n.r);
+            stack.push_back(n.l);
+        } else if (n.leaf > 0) {
+            if (n.r < 0) fail("negative triangle count");
+            for (int t = n.l; t < n.l + n.r; ++t) {
+                if (t < 0 || t >= I.num_tris) fail("leaf triangle index out of range: " + std::to_string(t));
+                tris_out.push_back(t);
+            }
+        } else {
+            fail("TLAS leaf inside a BLAS");
+        }
+    }
+}
+
+// Append a sah::Builder tree to I.bn; leaves through `leaf`.
+template <class LeafFn> int append_tree(Impl& I, const sah::Builder& B, LeafFn leaf) {
+    const int base = (int)I.bn.size();
+    I.bn.resize(base + B.nodes.size());
+    for (size_t i = 0; i < B.nodes.size(); ++i) {
+        const sah::Node& s = B.nodes[i];
+        BinNode& d = I.bn[base + i];
+        for (int k = 0; k < 3; ++k) { d.lo[k] = s.box.lo[k]; d.hi[k] = s.box.hi[k]; }
+        if (s.left < 0) {
+            leaf(s, d);
+        } else {
+            d.l = base + s.left;
+            d.r = base + s.right;
+            d.leaf = 0;
+        }
+    }
+    return base;  // the root (builder node 0)
+}
+
+void build_all(Impl& I, WideBVH* out) {
+    I.nodes.clear();
+    I.tris.clear();
+    I.insts.clear();
+    I.merged.clear();
+    I.blas_root_map.clear();
+    I.inst_identity.assign(I.num_instances, 0);
+    for (int i = 0; i < I.num_instances; ++i) {
+        InstXf xf;
+        int id = 0;
+        ptgb_instance_xf(&I.transforms[16 * (size_t)i], &xf, &id);
+        I.inst_identity[i] = id;
+    }
+    std::vector<int> leaves;
+    collect_tlas_leaves(I, I.top, leaves);
+    std::vector<int> ident, other;
+    for (int li : leaves) {
+        const int inst = -I.bn[li].leaf - 1;
+        if (inst >= I.num_instances) fail("instance index out of range: " + std::to_string(inst));
+        (I.inst_identity[inst] ? ident : other).push_back(li);
+    }
+    int tlas_root_bin = I.top;
+    const size_t input_nodes = I.bn.size();
+    if (ident.size() >= 2) {
+        // one BLAS over the triangles of every untransformed instance
+        sah::Builder M;
+        std::vector<MergedTri> prims;
+        std::vector<int> tl;
+        for (int li : ident) {
+            tl.clear();
+            collect_blas_tris(I, I.bn[li].l, tl);
+            for (int t : tl) prims.push_back({t, -I.bn[li].leaf - 1, I.bn[li].r});
+        }
+        M.refs.resize(prims.size());
+        for (size_t k = 0; k < prims.size(); ++k) {
+            Box b = tri_box(I, prims[k].tri);
+            sah::Ref& r = M.refs[k];
+            for (int j = 0; j < 3; ++j) {
+                r.b.lo[j] = b.lo[j];
+                r.b.hi[j] = b.hi[j];
+                r.c[j] = 0.5f * (b.lo[j] + b.hi[j]);
+            }
+            r.idx = (int)k;
+        }
+        if (!prims.empty()) {
+            M.nodes.reserve(2 * prims.size());
+            M.build(0, (int)prims.size());
+            I.merged.resize(prims.size());
+            for (size_t k = 0; k < M.packed.size(); ++k) I.merged[k] = prims[M.packed[k]];
+            const int merged_root = append_tree(I, M, [](const sah::Node& s, BinNode& d) {
+                d.l = s.start;
+                d.r = s.count;
+                d.leaf = 2;
+            });
+            // TLAS over the merged BLAS and the transformed instances
+            sah::Builder T;
+            T.max_leaf = 1;
+            std::vector<int> items;  // TLAS leaf node per item; -1 = merged BLAS
+            items.push_back(-1);
+            for (int li : other) items.push_back(li);
+            T.refs.resize(items.size());
+            for (size_t k = 0; k < items.size(); ++k) {
+                sah::Ref& r = T.refs[k];
+                const float* lo = items[k] < 0 ? I.bn[merged_root].lo : I.bn[items[k]].lo;
+                const float* hi = items[k] < 0 ? I.bn[merged_root].hi : I.bn[items[k]].hi;
+                for (int j = 0; j < 3; ++j) {
+                    r.b.lo[j] = lo[j];
+                    r.b.hi[j] = hi[j];
+                    r.c[j] = 0.5f * (lo[j] + hi[j]);
+                }
+                r.idx = (int)k;
+            }
+            T.nodes.reserve(2 * items.size());
+            T.build(0, (int)items.size());
+            tlas_root_bin = append_tree(I, T, [&](const sah::Node& s, BinNode& d) {
+                const int it = items[T.packed[s.start]];
+                if (it < 0) {
+                    d.l = merged_root;
+                    d.r = -1;
+                    d.leaf = -kMergedInstance - 1;
+                } else {
+                    d = I.bn[it];
+                }
+            });
+        }
+    }
+    // BLASes referenced by the TLAS, then the TLAS
+    std::vector<int> tl_leaves;
+    collect_tlas_leaves(I, tlas_root_bin, tl_leaves);
+    I.tlas = false;
+    I.max_depth = 0;
+    for (int li : tl_leaves) {
+        const int r = I.bn[li].l;
+        if (I.blas_root_map.count(r)) continue;
+        if (I.bn[r].leaf < 0) fail("BLAS root is a TLAS leaf");
+        I.blas_root_map[r] = build_root(I, r);
+    }
+    out->blas_depth = I.max_depth;
+    I.max_depth = 0;
+    I.tlas = true;
+    out->tlas_first_node = (int)I.nodes.size();
+    out->tlas_root = build_root(I, tlas_root_bin);
+    out->tlas_depth = I.max_depth;
+    I.bn.resize(input_nodes);  // drop the appended trees: the input stays as given
     out->nodes = I.nodes.data();
     out->num_nodes = (int)I.nodes.size();
     out->tris = I.tris.data();
@@ -393,21 +570,8 @@ void publish(Impl& I, WideBVH* out) {
     out->impl = &I;
 }
 
-void set_identity(Impl& I, const float* transforms, int num_instances) {
-    I.num_instances = num_instances;
-    I.inst_identity.assign(num_instances, 0);
-    for (int i = 0; i < num_instances; ++i) {
-        InstXf xf;
-        int id = 0;
-        ptgb_instance_xf(transforms + 16 * (size_t)i, &xf, &id);
-        I.inst_identity[i] = id;
-    }
-}
-
 void copy_err(const std::string& m, char* err, int n) {
-    if (err && n > 0) {
-        std::snprintf(err, n, "%s", m.c_str());
-    }
+    if (err && n > 0) std::snprintf(err, n, "%s", m.c_str());
 }
 
 }  // namespace
@@ -470,29 +634,19 @@ extern "C" int ptgb_build_wide(const float* bvh_nodes, int num_bvh_nodes, int to
     try {
         if (!bvh_nodes || num_bvh_nodes <= 0) fail("no BVH nodes");
         if (top_level_index < 0 || top_level_index >= num_bvh_nodes) fail("top_level_index out of range");
-        read_binary(*I, bvh_nodes, num_bvh_nodes);
-        I->vidx = vert_indices;
-        I->verts = vertices_uvx;
+        if (num_tris < 0 || num_vertices < 0 || num_instances <= 0) fail("negative sizes");
+        I->bn.resize(num_bvh_nodes);
+        read_binary(I->bn, bvh_nodes, 0, num_bvh_nodes);
+        I->top = top_level_index;
+        I->vidx.assign(vert_indices, vert_indices + 3 * (size_t)num_tris);
+        I->verts.resize(3 * (size_t)num_vertices);
+        for (int v = 0; v < num_vertices; ++v)
+            for (int k = 0; k < 3; ++k) I->verts[3 * (size_t)v + k] = vertices_uvx[4 * (size_t)v + k];
         I->num_tris = num_tris;
         I->num_vertices = num_vertices;
-        set_identity(*I, transforms, num_instances);
-        std::vector<int> roots;
-        collect_blas_roots(*I, top_level_index, roots);
-        I->tlas = false;
-        for (int r : roots) {
-            if (I->blas_root_map.count(r)) continue;
-            if (I->bn[r].leaf < 0) fail("BLAS root is a TLAS leaf");
-            I->blas_root_map[r] = build_root(*I, r);
-        }
-        I->blas_node_count = (int)I->nodes.size();
-        I->blas_tri_count = (int)I->tris.size();
-        out->blas_depth = I->max_depth;
-        I->max_depth = 0;
-        I->tlas = true;
-        out->tlas_first_node = (int)I->nodes.size();
-        out->tlas_root = build_root(*I, top_level_index);
-        out->tlas_depth = I->max_depth;
-        publish(*I, out);
+        I->num_instances = num_instances;
+        I->transforms.assign(transforms, transforms + 16 * (size_t)num_instances);
+        build_all(*I, out);
         return PT_OK;
     } catch (const BuildError& e) {
         copy_err(e.msg, err, err_size);
@@ -513,33 +667,28 @@ extern "C" int ptgb_rebuild_tlas(WideBVH* out, const float* bvh_nodes, int num_b
     if (!I) { copy_err("no BVH to update", err, err_size); return PT_ERR_INVALID_ARG; }
     try {
         if (top_level_index < 0 || top_level_index >= num_bvh_nodes) fail("top_level_index out of range");
+        if (top_level_index != I->top) fail("the BLAS part of the BVH changed size");
+        if (num_instances <= 0) fail("no instances");
         // the BLAS part of the binary array is unchanged (Scene::RebuildInstances
-        // rewrites only the TLAS slice, Scene.cpp:200-214)
-        if ((int)I->bn.size() < num_bvh_nodes) I->bn.resize(num_bvh_nodes);
-        for (int i = top_level_index; i < num_bvh_nodes; ++i) {
-            const float* p = bvh_nodes + 9 * (size_t)i;
-            BinNode& b = I->bn[i];
-            for (int k = 0; k < 3; ++k) { b.lo[k] = p[k]; b.hi[k] = p[3 + k]; }
-            b.l = (int)p[6]; b.r = (int)p[7]; b.leaf = (int)p[8];
-        }
-        set_identity(*I, transforms, num_instances);
-        I->nodes.resize(I->blas_node_count);
-        I->tris.resize(I->blas_tri_count);
-        I->insts.clear();
-        std::vector<int> roots;
-        collect_blas_roots(*I, top_level_index, roots);
-        for (int r : roots)
-            if (!I->blas_root_map.count(r)) fail("TLAS refers to a BLAS that was not in the original scene");
-        I->tlas = true;
-        I->max_depth = 0;
-        out->tlas_first_node = (int)I->nodes.size();
-        out->tlas_root = build_root(*I, top_level_index);
-        out->tlas_depth = I->max_depth;
-        publish(*I, out);
+        // rewrites only the TLAS slice, Scene.cpp:200-214); the build runs on a
+        // copy so that a rejected update leaves the current BVH in place
+        Impl next = *I;
+        next.bn.resize(num_bvh_nodes);
+        read_binary(next.bn, bvh_nodes, top_level_index, num_bvh_nodes);
+        next.num_instances = num_instances;
+        next.transforms.assign(transforms, transforms + 16 * (size_t)num_instances);
+        WideBVH tmp = *out;
+        build_all(next, &tmp);
+        *I = std::move(next);  // moving the vectors keeps their buffers, so tmp's pointers stay valid
+        tmp.impl = I;
+        *out = tmp;
         return PT_OK;
     } catch (const BuildError& e) {
         copy_err(e.msg, err, err_size);
         return PT_ERR_INVALID_ARG;
+    } catch (const std::bad_alloc&) {
+        copy_err("host allocation failed in BVH collapse", err, err_size);
+        return PT_ERR_OUT_OF_MEMORY;
     }
 }
 

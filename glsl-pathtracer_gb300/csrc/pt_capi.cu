@@ -171,6 +171,16 @@ int check_options(const pt_render_options* o) {
     return PT_OK;
 }
 
+// TLAS leaves (LRLeaf.z < 0) carry the instance's material index in LRLeaf.y.
+int check_tlas_materials(const float* tlas_nodes, int n, int num_materials) {
+    for (int i = 0; i < n; ++i) {
+        const float* p = tlas_nodes + 9 * (size_t)i;
+        if (p[8] < 0.0f && (p[7] < 0.0f || p[7] >= (float)num_materials))
+            return set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
+    }
+    return PT_OK;
+}
+
 int upload_instances(pt_context* c, const float* transforms, int n) {
     std::vector<InstXf> xf(n);
     for (int i = 0; i < n; ++i) {
@@ -324,13 +334,9 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
                              d->vertices_uvx, d->num_vertices, d->transforms, d->num_instances, &c->bvh, msg,
                              sizeof msg);
         if (rc) { set_err(rc, std::string("BVH: ") + msg); break; }
-        for (int i = 0; i < c->bvh.num_inst_refs; ++i) {
-            if (c->bvh.insts[i].material < 0 || c->bvh.insts[i].material >= d->num_materials) {
-                rc = set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
-                break;
-            }
-        }
-        if (rc) break;
+        if ((rc = check_tlas_materials(d->bvh_nodes + 9 * (size_t)d->top_level_index,
+                                       d->num_bvh_nodes - d->top_level_index, d->num_materials)))
+            break;
         c->bin_nodes.assign(d->bvh_nodes, d->bvh_nodes + 9 * (size_t)d->num_bvh_nodes);
         c->top_level_index = d->top_level_index;
         c->num_tris = d->num_tris;
@@ -429,17 +435,16 @@ int pt_update_instances(pt_context* c, const float* transforms, int32_t num_inst
         if (num_materials <= 0) return set_err(PT_ERR_INVALID_ARG, "num_materials must be positive");
         if (int rc = check_materials(materials, num_materials)) return rc;
     }
+    int rc = check_tlas_materials(tlas_nodes, num_tlas_nodes, materials ? num_materials : c->num_materials);
+    if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
-    c->bin_nodes.resize(9 * (size_t)(c->top_level_index + num_tlas_nodes));
-    std::memcpy(c->bin_nodes.data() + 9 * (size_t)c->top_level_index, tlas_nodes, 9 * sizeof(float) * num_tlas_nodes);
+    std::vector<float> bin(c->bin_nodes.begin(), c->bin_nodes.begin() + 9 * (size_t)c->top_level_index);
+    bin.insert(bin.end(), tlas_nodes, tlas_nodes + 9 * (size_t)num_tlas_nodes);
     char msg[512] = {0};
-    int rc = ptgb_rebuild_tlas(&c->bvh, c->bin_nodes.data(), c->top_level_index + num_tlas_nodes, c->top_level_index,
-                               transforms, num_instances, msg, sizeof msg);
+    rc = ptgb_rebuild_tlas(&c->bvh, bin.data(), c->top_level_index + num_tlas_nodes, c->top_level_index, transforms,
+                           num_instances, msg, sizeof msg);
     if (rc) return set_err(rc, std::string("TLAS: ") + msg);
-    const int nm = materials ? num_materials : c->num_materials;
-    for (int i = 0; i < c->bvh.num_inst_refs; ++i)
-        if (c->bvh.insts[i].material < 0 || c->bvh.insts[i].material >= nm)
-            return set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
+    c->bin_nodes.swap(bin);
     c->num_instances = num_instances;
     if ((rc = upload_bvh(c))) return rc;
     if ((rc = upload_instances(c, transforms, num_instances))) return rc;

@@ -54,7 +54,11 @@ __device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
     return r;
 }
 
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+#ifdef __CUDA_ARCH__
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+#endif
+}
 
 // Byte j of w as a float, without the (quarter-rate) integer conversion:
 // the byte becomes the low mantissa bits of 2^23, which is then subtracted.
@@ -122,7 +126,7 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
 //   T > det * tmax * (1 + 1e-6)  t rounds to above tmax;
 // each of these implies the full test fails, so the accepted set is unchanged.
 __device__ __forceinline__ bool tri_test(const TRay& r, const float4* __restrict__ tris, int t, float tmax, float& u,
-                                         float& v, float& tt, float& w, int& prim) {
+                                         float& v, float& tt, float& w, int& prim, int& tinst, int& tmat) {
     const float4 a = __ldg(tris + 3 * (size_t)t), b = __ldg(tris + 3 * (size_t)t + 1),
                  c = __ldg(tris + 3 * (size_t)t + 2);
     // e0 = b, e1 = c (precomputed v1-v0, v2-v0)
@@ -154,6 +158,8 @@ __device__ __forceinline__ bool tri_test(const TRay& r, const float4* __restrict
     tt = __fdiv_rn(T, det);
     w = __fsub_rn(__fsub_rn(1.0f, u), v);
     prim = __float_as_int(a.w);
+    tinst = __float_as_int(b.w);
+    tmat = __float_as_int(c.w);
     return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < tmax;
 }
 
@@ -216,6 +222,9 @@ __device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp
 
 // One step.  ANY: stop at the first accepted triangle (any-hit query);
 // ALPHA (with ANY): anyhit.glsl:118-141's alpha test, drawing from rng.
+// A step tests one triangle, enters one instance, or picks the nearest
+// internal child of the current node group -- popping the next group off
+// the stack first when the current one is exhausted -- and intersects it.
 template <bool ANY, bool ALPHA>
 __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng) {
     const bool in_blas = s.cur_inst >= 0;
@@ -225,11 +234,14 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         if (in_blas) {
             if (s.pbits) prefetch_l1(P.tris + 3 * (size_t)(s.pbase + __ffs(s.pbits) - 1));
             float u, v, t, w;
-            int prim;
-            if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim)) {
+            int prim, tinst, tmat;
+            if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim, tinst, tmat)) {
+                // the merged BLAS of untransformed instances (cur_mat < 0)
+                // carries instance and material per triangle
+                const int mat = s.cur_mat < 0 ? tmat : s.cur_mat;
                 if (ANY) {
                     if (!ALPHA) return TRAV_HIT;
-                    const float4 ap = __ldg(P.mats + 8 * s.cur_mat + 7);  // opacity, alphaMode, cutoff
+                    const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
                     const int alphaMode = (int)ap.y;
                     bool skip = alphaMode == ALPHA_MODE_MASK && ap.x < ap.z;
                     if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > ap.x;
@@ -239,8 +251,8 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                     s.u = u;
                     s.v = v;
                     s.prim = prim;
-                    s.inst = s.cur_inst;
-                    s.mat = s.cur_mat;
+                    s.inst = s.cur_mat < 0 ? tinst : s.cur_inst;
+                    s.mat = mat;
                 }
             }
         } else {
@@ -259,7 +271,21 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         }
         return TRAV_RUNNING;
     }
-    if (s.next < 0 && s.ng.y > 0x00ffffffu) {
+    if (s.next < 0) {
+        if (s.ng.y <= 0x00ffffffu) {  // the current group is exhausted: pop
+            if (s.sp == 0) return TRAV_DONE;
+            const uint2 e = stack[--s.sp];
+            if (e.x == kBlasSentinel) {  // back to the TLAS
+                const uint2 pend = stack[--s.sp];
+                s.ng = stack[--s.sp];
+                s.pbase = pend.x;
+                s.pbits = pend.y;
+                s.cur_inst = -1;
+                s.cur = prep_ray(s.wo, s.wd);
+                return TRAV_RUNNING;
+            }
+            s.ng = e;  // groups on the stack always hold internal children
+        }
         const uint32_t bit = 31u - __clz(s.ng.y);
         const uint32_t slot = (bit - 24u) ^ s.cur.oct_inv;
         const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << slot));
@@ -267,40 +293,22 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         s.ng.y &= ~(1u << bit);
         if (s.ng.y > 0x00ffffffu) trav_push(P, stack, s.sp, s.ng);
     }
-    if (s.next >= 0) {
-        uint32_t cb, pb, im;
-        const uint32_t hm = intersect_node(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
-        s.next = -1;
-        s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
-        s.pbase = pb;
-        s.pbits = hm & 0x00ffffffu;
-        if (s.pbits) {  // the next step tests a triangle (or enters an instance)
-            if (in_blas) prefetch_l1(P.tris + 3 * (size_t)(pb + __ffs(s.pbits) - 1));
-        } else if (s.ng.y > 0x00ffffffu) {  // or intersects the nearest child
-            const uint32_t bit = 31u - __clz(s.ng.y);
-            const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << ((bit - 24u) ^ s.cur.oct_inv)));
-            const char* np = reinterpret_cast<const char*>(P.nodes + (size_t)(cb + rel) * 5);
-            prefetch_l1(np);
-            prefetch_l1(np + 64);
-        }
-        return TRAV_RUNNING;
+    uint32_t cb, pb, im;
+    const uint32_t hm = intersect_node(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
+    s.next = -1;
+    s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
+    s.pbase = pb;
+    s.pbits = hm & 0x00ffffffu;
+    if (s.pbits) {  // the next step tests a triangle (or enters an instance)
+        if (in_blas) prefetch_l1(P.tris + 3 * (size_t)(pb + __ffs(s.pbits) - 1));
+    } else if (s.ng.y > 0x00ffffffu) {  // or intersects the nearest child
+        const uint32_t bit = 31u - __clz(s.ng.y);
+        const uint32_t rel = __popc(s.ng.y & ~(0xffffffffu << ((bit - 24u) ^ s.cur.oct_inv)));
+        const char* np = reinterpret_cast<const char*>(P.nodes + (size_t)(cb + rel) * 5);
+        prefetch_l1(np);
+        prefetch_l1(np + 64);
     }
-    // the current group is exhausted: pop
-    if (s.sp > 0) {
-        const uint2 e = stack[--s.sp];
-        if (e.x == kBlasSentinel) {  // back to the TLAS
-            const uint2 pend = stack[--s.sp];
-            s.ng = stack[--s.sp];
-            s.pbase = pend.x;
-            s.pbits = pend.y;
-            s.cur_inst = -1;
-            s.cur = prep_ray(s.wo, s.wd);
-        } else {
-            s.ng = e;
-        }
-        return TRAV_RUNNING;
-    }
-    return TRAV_DONE;
+    return TRAV_RUNNING;
 }
 
 // Closest triangle hit along (o, d) closer than tmax: fills s.prim (-1 if

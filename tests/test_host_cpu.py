@@ -144,6 +144,9 @@ def collapse(sd):
     return nodes, tris, insts, info
 
 
+MERGED_INSTANCE = 0x7FFFFFFF  # InstRef.instance of the BLAS merging all untransformed instances
+
+
 def decode(node):
     p = node[0:3].view(np.float32).astype(np.float64)
     e = [(int(node[3]) >> (8 * k)) & 0xFF for k in range(3)]
@@ -168,8 +171,24 @@ def test_wide_bvh_collapse_is_conservative_and_complete(which):
     V = sd.vertices_uvx[:, :3].astype(np.float64)
     seen_tris = np.zeros(len(tris), int)
     seen_inst = np.zeros(len(insts), int)
+    pairs = []  # (instance, reference triangle) reached through the wide tree
+    # the reference's TLAS leaves: instance -> (BLAS root, material)
+    bn = sd.bvh_nodes
+    leaf_of = {}
+    for i in range(sd.top_level_index, bn.shape[0]):
+        if bn[i, 8] < 0:
+            leaf_of[int(-bn[i, 8]) - 1] = (int(bn[i, 6]), int(bn[i, 7]))
+    expected = set()
+    for inst, (root, _) in leaf_of.items():
+        stack = [root]
+        while stack:
+            b = stack.pop()
+            if bn[b, 8] == 0:
+                stack += [int(bn[b, 6]), int(bn[b, 7])]
+            else:
+                expected |= {(inst, t) for t in range(int(bn[b, 6]), int(bn[b, 6]) + int(bn[b, 7]))}
 
-    def walk(idx, tlas, xf=None):
+    def walk(idx, tlas, xf=None, inst=None):
         """Checks the subtree of wide node idx; returns the exact bounds of
         its triangles (world space for the TLAS)."""
         d = decode(nodes[idx])
@@ -184,7 +203,7 @@ def test_wide_bvh_collapse_is_conservative_and_complete(which):
             if d["imask"] >> s & 1:
                 assert m == (1 << 5) | (24 + s)
                 rel = bin(d["imask"] & ((1 << s) - 1)).count("1")
-                c_lo, c_hi = walk(d["child_base"] + rel, tlas, None)
+                c_lo, c_hi = walk(d["child_base"] + rel, tlas, None, inst)
             else:
                 cnt = {1: 1, 3: 2, 7: 3}[m >> 5]
                 off = m & 31
@@ -194,12 +213,25 @@ def test_wide_bvh_collapse_is_conservative_and_complete(which):
                     if tlas:
                         seen_inst[pi] += 1
                         ir = insts[pi]
-                        M = sd.transforms[ir[1]].reshape(4, 4).astype(np.float64)
-                        b_lo, b_hi = walk(ir[0], False, M)
+                        if ir[1] == MERGED_INSTANCE:  # untransformed instances merged into one BLAS
+                            assert ir[2] == -1 and ir[3] == 1
+                            M = np.eye(4)
+                        else:
+                            M = sd.transforms[ir[1]].reshape(4, 4).astype(np.float64)
+                            assert ir[2] == leaf_of[ir[1]][1]
+                        b_lo, b_hi = walk(ir[0], False, M, int(ir[1]))
                     else:
                         seen_tris[pi] += 1
                         t = tris[pi]
-                        vi = sd.vert_indices[int(t[3:4].view(np.int32)[0])]
+                        prim = int(t[3:4].view(np.int32)[0])
+                        if inst == MERGED_INSTANCE:
+                            ti, tm = int(t[7:8].view(np.int32)[0]), int(t[11:12].view(np.int32)[0])
+                            assert np.array_equal(sd.transforms[ti], np.eye(4, dtype=np.float32).ravel())
+                            assert tm == leaf_of[ti][1]
+                            pairs.append((ti, prim))
+                        else:
+                            pairs.append((inst, prim))
+                        vi = sd.vert_indices[prim]
                         P = V[vi]
                         # (v0, e0, e1) are the reference's v0, v1-v0, v2-v0
                         assert np.array_equal(t[0:3], sd.vertices_uvx[vi[0], :3])
@@ -225,7 +257,10 @@ def test_wide_bvh_collapse_is_conservative_and_complete(which):
     walk(info["tlas_root"], True)
     assert np.all(seen_inst == 1)
     assert np.all(seen_tris >= 1)
-    # every reference triangle of every referenced BLAS is in the wide array
-    prims = np.sort(tris[:, 3].view(np.int32))
-    assert np.array_equal(np.unique(prims), prims)
+    # every (instance, triangle) pair of the reference's two-level tree is
+    # reached exactly once
+    assert len(pairs) == len(set(pairs))
+    assert set(pairs) == expected
     assert info["blas_depth"] + info["tlas_depth"] <= 48
+    if which == "icosphere":  # all instances untransformed: one merged BLAS
+        assert len(insts) == 1 and insts[0, 1] == MERGED_INSTANCE
