@@ -203,7 +203,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="icosphere_1m", choices=sorted(CONFIGS))
-    ap.add_argument("--integrator", default="megakernel", choices=["megakernel", "wavefront"])
+    ap.add_argument("--integrator", default="wavefront", choices=["megakernel", "wavefront"])
+    ap.add_argument("--compare-steps", type=int, default=3,
+                    help="timed steps of the other integrator, for the wavefront/megakernel ratio (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
     ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
@@ -250,6 +252,7 @@ def main():
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     rays = 0
+    launches = 0
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -260,6 +263,7 @@ def main():
                 ends[k].record(stream)
             st = r.stats()  # synchronises; counters of this launch
             rays += st["closest"] + st["shadow"]
+            launches += st["launches"]
             if st["status"] != 0:
                 raise RuntimeError(f"kernel status {st['status']}")
         torch.cuda.synchronize()
@@ -275,6 +279,33 @@ def main():
         t_total, rays = float(tmax[0]), int(t[1])
     value = rays / t_total / 1e6
     rays_per_step = rays / (args.steps * world)
+
+    # the other integrator on the same frame, same timing rules (the two give
+    # the same accumulation bit for bit on this scene, so equal RMSE)
+    other = None
+    if args.compare_steps > 0:
+        other_name = "megakernel" if args.integrator == "wavefront" else "wavefront"
+        r.set_integrator(capi.PT_INTEGRATOR_MEGAKERNEL if other_name == "megakernel" else capi.PT_INTEGRATOR_WAVEFRONT)
+        base2 = pass_base + (args.warmup + 2 * args.steps + 4) * spp
+        with torch.cuda.stream(stream):
+            r.render_passes(base2, spp)  # warm-up
+        torch.cuda.synchronize()
+        o_ms, o_rays = 0.0, 0
+        for k in range(args.compare_steps):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                ev0.record(stream)
+                r.render_passes(base2 + (k + 1) * spp, spp)
+                ev1.record(stream)
+            st = r.stats()
+            o_rays += st["closest"] + st["shadow"]
+            o_ms += ev0.elapsed_time(ev1)
+        o_val = o_rays / (o_ms / 1000.0) / 1e6
+        other = {"integrator": other_name, "value": o_val, "unit": "Mrays/s", "steps": args.compare_steps,
+                 "ms_per_step": o_ms / args.compare_steps,
+                 "wavefront_over_megakernel": (value / o_val) if other_name == "megakernel" else (o_val / value)}
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else capi.PT_INTEGRATOR_MEGAKERNEL)
 
     # end to end through the C ABI with host buffers
     import ctypes as C
@@ -320,13 +351,15 @@ def main():
                        "integrator": args.integrator, "rays_per_step": rays_per_step,
                        "l2": "flushed before each timed step (512 MiB write)",
                        "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU"},
-            "gpu_launches": args.steps * world,
+            "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "bytes_per_ray": b_ray, **work},
             "e2e": e2e,
             "clocks": clk.summary(),
         }
+        if other:
+            line["compare"] = other
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))

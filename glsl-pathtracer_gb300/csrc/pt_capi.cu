@@ -98,6 +98,9 @@ struct pt_context {
     WavefrontBuffers wf;
     WavefrontTuning wf_tuning;
     bool wf_tuned = false;
+    int launches = 0;  // kernels launched by the last render call
+    bool stage_timing = false;
+    StageTimer timer;
 };
 
 namespace {
@@ -285,9 +288,14 @@ int render(pt_context* c, const RenderWork& w) {
         }
         const char* g = std::getenv("PT_WAVEFRONT_GRAPH");
         const bool use_graph = !(g && g[0] == '0');
-        CK(launch_wavefront(p, w, c->wf, c->wf_tuning, use_graph, c->stream));
+        WavefrontTuning t = c->wf_tuning;
+        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+        c->timer.reset();
+        CK(launch_wavefront(p, w, c->wf, t, use_graph, c->stream, &c->launches,
+                            c->stage_timing ? &c->timer : nullptr));
     } else {
         CK(launch_render(p, w, c->integrator, c->stream));
+        c->launches = 1;
     }
     return end_launch(c);
 }
@@ -388,6 +396,7 @@ int pt_destroy(pt_context* c) {
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
     c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();
     wavefront_free(c->wf);
+    c->timer.release();
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -574,6 +583,69 @@ int pt_trace_shadow(pt_context* c, const pt_ray* rays, const float* maxd, int32_
     return PT_OK;
 }
 
+int pt_bsdf_eval(pt_context* c, const float* rec, const float* V, const float* N, const float* L, int32_t n,
+                 float* f, float* pdf) {
+    if (!c || n < 0 || (n && (!rec || !V || !N || !L || !f || !pdf)))
+        return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    if (!n) return PT_OK;
+    DevBuf<float> dr, dv, dn, dl, df, dp;
+    CK(dr.upload(rec, 20 * (size_t)n, c->stream));
+    CK(dv.upload(V, 3 * (size_t)n, c->stream));
+    CK(dn.upload(N, 3 * (size_t)n, c->stream));
+    CK(dl.upload(L, 3 * (size_t)n, c->stream));
+    CK(df.alloc(3 * (size_t)n));
+    CK(dp.alloc(n));
+    CK(launch_bsdf_eval(dr.p, dv.p, dn.p, dl.p, n, df.p, dp.p, c->stream));
+    CK(cudaMemcpyAsync(f, df.p, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(pdf, dp.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto* b : {&dr, &dv, &dn, &dl, &df, &dp}) b->free();
+    return PT_OK;
+}
+
+int pt_bsdf_sample(pt_context* c, const float* rec, const float* V, const float* N, const uint32_t* seeds, int32_t n,
+                   float* L, float* f, float* pdf) {
+    if (!c || n < 0 || (n && (!rec || !V || !N || !seeds || !L || !f || !pdf)))
+        return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    if (!n) return PT_OK;
+    DevBuf<float> dr, dv, dn, dl, df, dp;
+    DevBuf<uint32_t> ds;
+    CK(dr.upload(rec, 20 * (size_t)n, c->stream));
+    CK(dv.upload(V, 3 * (size_t)n, c->stream));
+    CK(dn.upload(N, 3 * (size_t)n, c->stream));
+    CK(ds.upload(seeds, 4 * (size_t)n, c->stream));
+    CK(dl.alloc(3 * (size_t)n));
+    CK(df.alloc(3 * (size_t)n));
+    CK(dp.alloc(n));
+    CK(launch_bsdf_sample(dr.p, dv.p, dn.p, ds.p, n, dl.p, df.p, dp.p, c->stream));
+    CK(cudaMemcpyAsync(L, dl.p, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(f, df.p, 3 * sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(pdf, dp.p, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto* b : {&dr, &dv, &dn, &dl, &df, &dp}) b->free();
+    ds.free();
+    return PT_OK;
+}
+
+int pt_set_stage_timing(pt_context* c, int32_t on) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    c->stage_timing = on != 0;
+    c->timer.reset();
+    return PT_OK;
+}
+
+int pt_get_stage_stats(pt_context* c, pt_stage_stats* s) {
+    if (!c || !s) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    float ms[STAGE_COUNT];
+    int n[STAGE_COUNT];
+    CK(c->timer.summarise(ms, n));
+    for (int k = 0; k < STAGE_COUNT; ++k) {
+        s->ms[k] = ms[k];
+        s->launches[k] = n[k];
+    }
+    return PT_OK;
+}
+
 int pt_get_stats(pt_context* c, pt_stats* s) {
     if (!c || !s) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     unsigned long long cnt[3] = {0, 0, 0};
@@ -588,6 +660,7 @@ int pt_get_stats(pt_context* c, pt_stats* s) {
     s->paths = cnt[2];
     s->kernel_ms = ms;
     s->status = st;
+    s->kernel_launches = c->launches;
     return PT_OK;
 }
 

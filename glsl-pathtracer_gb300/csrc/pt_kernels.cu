@@ -5,6 +5,8 @@
 //                        the sample passes of the launch; shadow rays inline
 //   trace_closest_kernel test hook: ClosestHit's triangle part on a ray set
 //   trace_shadow_kernel  test hook: AnyHit's triangle part on a ray set
+//   bsdf_eval_kernel,    test hooks: DisneyEval / DisneySample
+//   bsdf_sample_kernel   (disney.glsl:142-351) on explicit inputs
 //   tonemap_kernel       tonemap.glsl:main + the RGBA8 read-back format
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -86,6 +88,75 @@ __global__ void __launch_bounds__(128) trace_shadow_kernel(Params P, const pt_ra
                        v3(rr.direction[0], rr.direction[1], rr.direction[2]), maxd[i], alpha, rng, stack)
                  ? 1
                  : 0;
+}
+
+// BSDF inputs: 20 floats per record (baseColor xyz, metallic, roughness,
+// subsurface, specularTint, sheen, sheenTint, clearcoat, clearcoatRoughness,
+// specTrans, ior, ax, ay, eta, anisotropic, 3 unused), as GetMaterial
+// leaves them after its remapping (pathtrace.glsl:25-115).
+__device__ __forceinline__ Material bsdf_material(const float* __restrict__ r, float& eta) {
+    Material m{};
+    m.baseColor = v3(r[0], r[1], r[2]);
+    m.metallic = r[3];
+    m.roughness = r[4];
+    m.subsurface = r[5];
+    m.specularTint = r[6];
+    m.sheen = r[7];
+    m.sheenTint = r[8];
+    m.clearcoat = r[9];
+    m.clearcoatRoughness = r[10];
+    m.specTrans = r[11];
+    m.ior = r[12];
+    m.ax = r[13];
+    m.ay = r[14];
+    eta = r[15];
+    m.anisotropic = r[16];
+    return m;
+}
+
+__device__ __forceinline__ V3 load_v3(const float* __restrict__ p, int i) {
+    return v3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+}
+
+__global__ void __launch_bounds__(128) bsdf_eval_kernel(const float* __restrict__ rec, const float* __restrict__ V,
+                                                        const float* __restrict__ N, const float* __restrict__ L,
+                                                        int n, float* __restrict__ f, float* __restrict__ pdf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float eta;
+    const Material m = bsdf_material(rec + 20 * (size_t)i, eta);
+    float p;
+    const V3 r = DisneyEval(m, eta, load_v3(V, i), load_v3(N, i), load_v3(L, i), p);
+    f[3 * i] = r.x;
+    f[3 * i + 1] = r.y;
+    f[3 * i + 2] = r.z;
+    pdf[i] = p;
+}
+
+__global__ void __launch_bounds__(128) bsdf_sample_kernel(const float* __restrict__ rec, const float* __restrict__ V,
+                                                          const float* __restrict__ N,
+                                                          const uint32_t* __restrict__ seeds, int n,
+                                                          float* __restrict__ L, float* __restrict__ f,
+                                                          float* __restrict__ pdf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float eta;
+    const Material m = bsdf_material(rec + 20 * (size_t)i, eta);
+    Rng rng;
+    rng.x = seeds[4 * i];
+    rng.y = seeds[4 * i + 1];
+    rng.z = seeds[4 * i + 2];
+    rng.w = seeds[4 * i + 3];
+    float p;
+    V3 l;
+    const V3 r = DisneySample(m, eta, load_v3(V, i), load_v3(N, i), l, p, rng);
+    L[3 * i] = l.x;
+    L[3 * i + 1] = l.y;
+    L[3 * i + 2] = l.z;
+    f[3 * i] = r.x;
+    f[3 * i + 1] = r.y;
+    f[3 * i + 2] = r.z;
+    pdf[i] = p;
 }
 
 // tonemap.glsl:59-133 and the float->RGBA8 conversion of glGetTexImage.
@@ -172,6 +243,20 @@ cudaError_t launch_trace_shadow(const Params& p, const void* rays, const float* 
                                 cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     trace_shadow_kernel<<<(n + 127) / 128, 128, 0, s>>>(p, (const pt_ray*)rays, maxd, n, occ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bsdf_eval(const float* rec, const float* V, const float* N, const float* L, int n, float* f,
+                             float* pdf, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    bsdf_eval_kernel<<<(n + 127) / 128, 128, 0, s>>>(rec, V, N, L, n, f, pdf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bsdf_sample(const float* rec, const float* V, const float* N, const uint32_t* seeds, int n,
+                               float* L, float* f, float* pdf, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    bsdf_sample_kernel<<<(n + 127) / 128, 128, 0, s>>>(rec, V, N, seeds, n, L, f, pdf);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,11 @@ namespace ptgb {
 // Traversal stack entries per thread (node groups of the wide BVH; one per
 // wide level on the current path, TLAS + BLAS).
 constexpr int kStackSize = 48;
+// Postponing triangle tests (the wavefront's warp step modes) puts at most
+// one triangle group on the stack per wide level besides the node group, so
+// a BVH of depth d (TLAS + BLAS levels) with 2 d + 3 <= kStackSize never
+// overflows; deeper BVHs are traversed without postponing.
+constexpr bool trav_postpone_fits(int depth) { return 2 * depth + 3 <= kStackSize; }
 
 struct Params {
     // acceleration structure (bvh8.h)
@@ -65,6 +70,10 @@ cudaError_t launch_render(const Params& p, const RenderWork& w, int integrator, 
 cudaError_t launch_trace_closest(const Params& p, const void* rays, int n, void* hits, cudaStream_t s);
 cudaError_t launch_trace_shadow(const Params& p, const void* rays, const float* maxd, int n, unsigned char* occ,
                                 cudaStream_t s);
+cudaError_t launch_bsdf_eval(const float* rec, const float* V, const float* N, const float* L, int n, float* f,
+                             float* pdf, cudaStream_t s);
+cudaError_t launch_bsdf_sample(const float* rec, const float* V, const float* N, const uint32_t* seeds, int n,
+                               float* L, float* f, float* pdf, cudaStream_t s);
 cudaError_t launch_tonemap(const Params& p, int num_samples, int enable_tonemap, int enable_aces, int simple_aces,
                            int background, int transparent, const float* bg, unsigned char* out, cudaStream_t s);
 }  // namespace ptgb

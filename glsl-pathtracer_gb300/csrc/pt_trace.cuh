@@ -60,13 +60,34 @@ __device__ __forceinline__ void prefetch_l1(const void* p) {
 #endif
 }
 
-// Byte j of w as a float, without the (quarter-rate) integer conversion:
-// the byte becomes the low mantissa bits of 2^23, which is then subtracted.
-__device__ __forceinline__ float qbyte(uint32_t w, int j) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j)) - 8388608.0f;
+// Byte j of w in the low mantissa bits of 2^23 (the float 2^23 + byte),
+// without the (quarter-rate) integer conversion.
+__device__ __forceinline__ float qbyte_biased(uint32_t w, int j) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j));
+}
+
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+#else
+    return fminf(fminf(a, b), c);
+#endif
 }
 
 // Slab test of the eight children of wide node `idx`; returns the hit mask.
+// Plane distances are (q - 2^23 bias) * (scale / d) + (origin - o) / d; the
+// entry and exit distances are three-input max / min (sm_100+).
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
                                                    float tmax, uint32_t& child_base, uint32_t& prim_base,
                                                    uint32_t& imask) {
@@ -99,11 +120,14 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
         const uint32_t nzw = nz ? qhiz : qloz, fzw = nz ? qloz : qhiz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float tnx = fmaf(qbyte(nxw, j), adjx, orgx), tfx = fmaf(qbyte(fxw, j), adjx, orgx);
-            const float tny = fmaf(qbyte(nyw, j), adjy, orgy), tfy = fmaf(qbyte(fyw, j), adjy, orgy);
-            const float tnz = fmaf(qbyte(nzw, j), adjz, orgz), tfz = fmaf(qbyte(fzw, j), adjz, orgz);
-            const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-            const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+            const float tnx = fmaf(qbyte_biased(nxw, j) - 8388608.0f, adjx, orgx);
+            const float tfx = fmaf(qbyte_biased(fxw, j) - 8388608.0f, adjx, orgx);
+            const float tny = fmaf(qbyte_biased(nyw, j) - 8388608.0f, adjy, orgy);
+            const float tfy = fmaf(qbyte_biased(fyw, j) - 8388608.0f, adjy, orgy);
+            const float tnz = fmaf(qbyte_biased(nzw, j) - 8388608.0f, adjz, orgz);
+            const float tfz = fmaf(qbyte_biased(fzw, j) - 8388608.0f, adjz, orgz);
+            const float t0 = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
+            const float t1 = fmin3f(tfx, tfy, fminf(tfz, tmax));
             if (t0 <= t1) {
                 const uint32_t cb = (child_bits4 >> (8 * j)) & 0xffu;
                 const uint32_t bi = (bit_index4 >> (8 * j)) & 0xffu;
@@ -115,7 +139,8 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
 }
 
 // Triangle test of closest_hit.glsl:128-143 (accept when u, v, t and
-// w = 1-u-v are all >= 0 and t < tmax) with the reference's operation order
+// w = 1-u-v are all >= 0 and t <= tmax; the caller decides t == tmax) with
+// the reference's operation order
 // and no contraction.  The numerators U, V, T and det are computed first;
 // with det made positive (an exact sign flip of all four) a triangle is
 // rejected before dividing when
@@ -160,7 +185,7 @@ __device__ __forceinline__ bool tri_test(const TRay& r, const float4* __restrict
     prim = __float_as_int(a.w);
     tinst = __float_as_int(b.w);
     tmat = __float_as_int(c.w);
-    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < tmax;
+    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt <= tmax;
 }
 
 // GLSL mat4 * vec4 with the sum in column order, no contraction
@@ -220,14 +245,40 @@ __device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp
     else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
 }
 
+// Step modes.  TRAV_LANE: each lane takes its own next unit of work.  With
+// TRAV_NODES / TRAV_TRIS the warp has chosen one kind of work for all its
+// lanes: under TRAV_NODES a lane with triangles pending postpones them (the
+// group goes on the stack, to be popped later) when it has a node to go to,
+// and idles otherwise; under TRAV_TRIS only lanes with triangles pending do
+// anything.  Running one kind per warp step keeps the node and triangle code
+// from both executing, each for part of the warp, on the same step.
+enum { TRAV_LANE = 0, TRAV_NODES = 1, TRAV_TRIS = 2 };
+
+// A stack entry is a node group (y bits 24-31: internal children left), a
+// postponed triangle group (y bits 24-31 clear, triangle bits below), a BLAS
+// sentinel, or the TLAS position under a sentinel.
+__device__ __forceinline__ bool trav_has_tris(const Trav& s) { return s.pbits && s.cur_inst >= 0; }
+__device__ __forceinline__ bool trav_can_descend(const Trav& s) {
+    return !trav_has_tris(s) || s.ng.y > 0x00ffffffu;
+}
+
 // One step.  ANY: stop at the first accepted triangle (any-hit query);
 // ALPHA (with ANY): anyhit.glsl:118-141's alpha test, drawing from rng.
 // A step tests one triangle, enters one instance, or picks the nearest
 // internal child of the current node group -- popping the next group off
 // the stack first when the current one is exhausted -- and intersects it.
+// Closest hits: the nearest triangle wins; of triangles at exactly the same
+// distance, the one of smallest (triangle, instance) id, so the result does
+// not depend on the order in which triangles are tested.
 template <bool ANY, bool ALPHA>
-__device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng) {
+__device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng, int mode = TRAV_LANE) {
     const bool in_blas = s.cur_inst >= 0;
+    if (mode == TRAV_TRIS && !(s.pbits && in_blas)) return TRAV_RUNNING;
+    if (s.pbits && in_blas && mode == TRAV_NODES) {
+        if (s.ng.y <= 0x00ffffffu) return TRAV_RUNNING;  // nothing to descend into: wait for a triangle step
+        trav_push(P, stack, s.sp, make_uint2(s.pbase, s.pbits));  // postpone the triangles
+        s.pbits = 0;
+    }
     if (s.pbits) {
         const int b = __ffs(s.pbits) - 1;
         s.pbits &= s.pbits - 1;
@@ -239,19 +290,22 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 // the merged BLAS of untransformed instances (cur_mat < 0)
                 // carries instance and material per triangle
                 const int mat = s.cur_mat < 0 ? tmat : s.cur_mat;
+                const int inst = s.cur_mat < 0 ? tinst : s.cur_inst;
                 if (ANY) {
-                    if (!ALPHA) return TRAV_HIT;
-                    const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
-                    const int alphaMode = (int)ap.y;
-                    bool skip = alphaMode == ALPHA_MODE_MASK && ap.x < ap.z;
-                    if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > ap.x;
-                    if (!skip) return TRAV_HIT;
-                } else {
+                    if (t < s.tmax) {
+                        if (!ALPHA) return TRAV_HIT;
+                        const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
+                        const int alphaMode = (int)ap.y;
+                        bool skip = alphaMode == ALPHA_MODE_MASK && ap.x < ap.z;
+                        if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > ap.x;
+                        if (!skip) return TRAV_HIT;
+                    }
+                } else if (t < s.tmax || (s.prim >= 0 && (prim < s.prim || (prim == s.prim && inst < s.inst)))) {
                     s.tmax = t;
                     s.u = u;
                     s.v = v;
                     s.prim = prim;
-                    s.inst = s.cur_mat < 0 ? tinst : s.cur_inst;
+                    s.inst = inst;
                     s.mat = mat;
                 }
             }
@@ -284,7 +338,13 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 s.cur = prep_ray(s.wo, s.wd);
                 return TRAV_RUNNING;
             }
-            s.ng = e;  // groups on the stack always hold internal children
+            if (e.y <= 0x00ffffffu) {  // a postponed triangle group
+                s.pbase = e.x;
+                s.pbits = e.y;
+                s.ng = make_uint2(0, 0);
+                return TRAV_RUNNING;
+            }
+            s.ng = e;  // a node group (always holds internal children)
         }
         const uint32_t bit = 31u - __clz(s.ng.y);
         const uint32_t slot = (bit - 24u) ^ s.cur.oct_inv;
@@ -309,6 +369,14 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         prefetch_l1(np + 64);
     }
     return TRAV_RUNNING;
+}
+
+// The warp's step mode: triangle steps when at least `min_tris` of its
+// tracing lanes have triangles pending, or when no lane has a node to go to.
+__device__ __forceinline__ int trav_warp_mode(const Trav& s, bool tracing, int min_tris) {
+    const unsigned tri = __ballot_sync(0xffffffffu, tracing && trav_has_tris(s));
+    const unsigned desc = __ballot_sync(0xffffffffu, tracing && trav_can_descend(s));
+    return (__popc(tri) >= min_tris || desc == 0) ? TRAV_TRIS : TRAV_NODES;
 }
 
 // Closest triangle hit along (o, d) closer than tmax: fills s.prim (-1 if

@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdlib>
+
 #include "../../include/pt_cuda.h"
 #include "pt_integrator.cuh"
 #include "pt_wavefront.h"
@@ -122,12 +124,20 @@ __device__ __forceinline__ int fetch_work(int* counter, int n, bool need) {
     return k < n ? k : -1;
 }
 
-// Closest-hit queries of the queue.  Persistent: a thread whose ray is done
-// fetches the next one while the rest of its warp keeps traversing, so the
-// warp's lanes stay busy however unequal the rays are.
+// Persistent traversal loop shared by the extend and shadow stages.  Lanes
+// trace independently, one traversal step per iteration; retiring finished
+// rays and fetching new ones (divergent, memory-heavy code) runs for the
+// whole warp at once, only when at least `refill` lanes are idle -- or, once
+// the queue is empty, when all are.  This keeps that code from running for
+// one or two lanes on almost every iteration.
+__device__ __forceinline__ int refill_target(bool exhausted, int refill) { return exhausted ? 32 : refill; }
+
+// Closest-hit queries of the queue.  Persistent: threads keep taking rays
+// from the queue until it is empty, so a warp's lanes stay busy however
+// unequal the rays are.
 // Traversal is memory-latency bound: 8 blocks of 128 threads (64 registers)
 // keep 32 warps per SM in flight.
-__global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in) {
+__global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -140,24 +150,34 @@ __global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in) 
     HitRecord hr;
     float tl = PT_INF;
     int ray = -1;
+    bool tracing = false, exhausted = false;
     for (;;) {
-        const int k = fetch_work(B.counts + 4, n, ray < 0);
-        if (k >= 0) {
-            ray = B.q[in][k];
-            const float4 o = B.o[ray], d = B.d[ray];
-            const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
-            tl = LightsClosest(P, r, B.misc[ray].x, hr);
-            trav_init(s, P, r.origin, r.direction, tl);
-            cnt.closest++;
-        }
-        if (!__any_sync(0xffffffffu, ray >= 0)) break;
-        if (ray >= 0 && trav_step<false, false>(s, P, stack, nullptr) != TRAV_RUNNING) {
+        if (ray >= 0 && !tracing) {  // retire
             FinishClosest(s, tl, hr);
             B.h0[ray] = make_float4(hr.t, hr.u, hr.v, hr.w);
             B.h1[ray] = make_int4(hr.prim, hr.inst, hr.mat, (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 : 0));
             B.h2[ray] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
             ray = -1;
         }
+        if (!exhausted) {  // refill
+            const int k = fetch_work(B.counts + 4, n, ray < 0);
+            exhausted = __any_sync(0xffffffffu, ray < 0 && k < 0);
+            if (k >= 0) {
+                ray = B.q[in][k];
+                const float4 o = B.o[ray], d = B.d[ray];
+                const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
+                tl = LightsClosest(P, r, B.misc[ray].x, hr);
+                trav_init(s, P, r.origin, r.direction, tl);
+                tracing = true;
+                cnt.closest++;
+            }
+        }
+        if (!__any_sync(0xffffffffu, tracing)) break;
+        const int target = refill_target(exhausted, refill);
+        do {
+            const int mode = min_tris > 0 ? trav_warp_mode(s, tracing, min_tris) : TRAV_LANE;
+            if (tracing && trav_step<false, false>(s, P, stack, nullptr, mode) != TRAV_RUNNING) tracing = false;
+        } while (__popc(__ballot_sync(0xffffffffu, !tracing)) < target);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
@@ -216,9 +236,10 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
 }
 
 // Any-hit queries of the shadow queue (one or two rays per path: the env
-// sample first, then the light sample), persistent like wf_extend.  The
-// deferred form is used only when AnyHit draws no random numbers.
-__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B) {
+// sample first, then the light sample), persistent like wf_extend, with the
+// same batched retire / refill.  The deferred form is used only when AnyHit
+// draws no random numbers.
+__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refill, int min_tris) {
     uint2 stack[kStackSize];
     const int n = B.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
@@ -227,21 +248,12 @@ __global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B) {
     // per-thread stage: 0 start env ray, 1 tracing it, 2 start light ray,
     // 3 tracing it, 4 both resolved
     int path = -1, bits = 0, stage = 0;
-    bool occ0 = false, occ1 = false;
+    bool occ0 = false, occ1 = false, exhausted = false;
     V3 origin = v3(0.0f);
-    for (;;) {
-        const int k = fetch_work(B.counts + 5, n, path < 0);
-        if (k >= 0) {
-            path = B.qs[k];
-            const float4 so = B.so[path];
-            bits = __float_as_int(so.w);
-            origin = v3(so.x, so.y, so.z);
-            occ0 = occ1 = false;
-            stage = 0;
-        }
-        if (!__any_sync(0xffffffffu, path >= 0)) break;
-        if (path < 0) continue;
-        if (stage == 0 || stage == 2) {
+    // start the next ray of a lane waiting at stage 0 or 2 (a ray a light
+    // occludes, or one the path does not have, moves on without tracing)
+    auto start = [&]() {
+        if (path >= 0 && (stage == 0 || stage == 2)) {
             const int which = stage >> 1;
             if (bits & (1 << which)) {
                 const float4 d = which ? B.sd1[path] : B.sd0[path];
@@ -259,38 +271,70 @@ __global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B) {
                 stage += 2;
             }
         }
-        if (stage == 1 || stage == 3) {
-            const int st = trav_step<true, false>(s, P, stack, nullptr);
-            if (st != TRAV_RUNNING) {
-                if (stage == 1) occ0 = st == TRAV_HIT;
-                else occ1 = st == TRAV_HIT;
-                stage += 1;
+    };
+    // both rays resolved: radiance += Ld * T
+    auto resolve = [&]() {
+        if (path >= 0 && stage == 4) {
+            ShadowReq sr;
+            sr.n = bits & 3;
+            sr.adds = (bits >> 2) & 3;
+            if (sr.n & 1) {
+                const float4 c = B.sc0[path];
+                sr.contrib[0] = v3(c.x, c.y, c.z);
+            }
+            if (sr.n & 2) {
+                const float4 c = B.sc1[path];
+                sr.contrib[1] = v3(c.x, c.y, c.z);
+            }
+            const int i = path;
+            path = -1;
+            const float4 T = B.sT[i];
+            const V3 Ld = ResolveShadow(sr, occ0, occ1);
+            float4 L = B.L[i];
+            const V3 rad = AddScaled(v3(L.x, L.y, L.z), Ld, v3(T.x, T.y, T.z));
+            L.x = rad.x;
+            L.y = rad.y;
+            L.z = rad.z;
+            B.L[i] = L;
+            if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+        }
+    };
+    for (;;) {
+        // retire: lanes done with the env ray start the light ray, lanes done
+        // with both resolve; then refill the idle lanes
+        start();
+        resolve();
+        if (!exhausted) {
+            const int k = fetch_work(B.counts + 5, n, path < 0);
+            exhausted = __any_sync(0xffffffffu, path < 0 && k < 0);
+            if (k >= 0) {
+                path = B.qs[k];
+                const float4 so = B.so[path];
+                bits = __float_as_int(so.w);
+                origin = v3(so.x, so.y, so.z);
+                occ0 = occ1 = false;
+                stage = 0;
+                start();
+                start();
+                resolve();
             }
         }
-        if (stage != 4) continue;
-        // both rays resolved: radiance += Ld * T
-        ShadowReq sr;
-        sr.n = bits & 3;
-        sr.adds = (bits >> 2) & 3;
-        if (sr.n & 1) {
-            const float4 c = B.sc0[path];
-            sr.contrib[0] = v3(c.x, c.y, c.z);
+        const bool tracing = path >= 0 && (stage == 1 || stage == 3);
+        if (!__any_sync(0xffffffffu, path >= 0)) break;
+        const int target = refill_target(exhausted, refill);
+        bool busy = tracing;
+        while (__popc(__ballot_sync(0xffffffffu, !busy)) < target) {
+            const int mode = min_tris > 0 ? trav_warp_mode(s, busy, min_tris) : TRAV_LANE;
+            if (busy) {
+                const int st = trav_step<true, false>(s, P, stack, nullptr, mode);
+                if (st != TRAV_RUNNING) {
+                    if (stage == 1) occ0 = st == TRAV_HIT;
+                    else occ1 = st == TRAV_HIT;
+                    stage += 1;
+                    busy = false;
+                }
+            }
         }
-        if (sr.n & 2) {
-            const float4 c = B.sc1[path];
-            sr.contrib[1] = v3(c.x, c.y, c.z);
-        }
-        const int i = path;
-        path = -1;
-        const float4 T = B.sT[i];
-        const V3 Ld = ResolveShadow(sr, occ0, occ1);
-        float4 L = B.L[i];
-        const V3 rad = AddScaled(v3(L.x, L.y, L.z), Ld, v3(T.x, T.y, T.z));
-        L.x = rad.x;
-        L.y = rad.y;
-        L.z = rad.z;
-        B.L[i] = L;
-        if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
@@ -388,28 +432,87 @@ void wavefront_free(WavefrontBuffers& wb) {
     wb = WavefrontBuffers{};
 }
 
+cudaError_t StageTimer::mark(cudaStream_t s) {
+    if (used >= pool.size()) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        pool.push_back(e);
+    }
+    return cudaEventRecord(pool[used++], s);
+}
+
+cudaError_t StageTimer::summarise(float ms[STAGE_COUNT], int launches[STAGE_COUNT]) const {
+    for (int k = 0; k < STAGE_COUNT; ++k) {
+        ms[k] = 0.0f;
+        launches[k] = 0;
+    }
+    for (size_t i = 0; i < kinds.size() && 2 * i + 1 < used; ++i) {
+        cudaError_t e = cudaEventSynchronize(pool[2 * i + 1]);
+        if (e != cudaSuccess) return e;
+        float t = 0.0f;
+        if ((e = cudaEventElapsedTime(&t, pool[2 * i], pool[2 * i + 1])) != cudaSuccess) return e;
+        ms[kinds[i]] += t;
+        launches[kinds[i]] += 1;
+    }
+    return cudaSuccess;
+}
+
+void StageTimer::release() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    pool.clear();
+    reset();
+}
+
+// A launch bracketed by timer events (when timing).
+template <class F> static cudaError_t timed(StageTimer* timer, int kind, cudaStream_t s, F&& launch) {
+    cudaError_t e;
+    if (timer && (e = timer->mark(s)) != cudaSuccess) return e;
+    if ((e = launch()) != cudaSuccess) return e;
+    if (timer) {
+        if ((e = timer->mark(s)) != cudaSuccess) return e;
+        timer->kinds.push_back(kind);
+    }
+    return cudaSuccess;
+}
+
 // Enqueue one batch: passes [first_pass, first_pass + npass) of the pixels of W.
 static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const WavefrontBuffers& wb, int first_pass,
-                                 int npass, int iterations, const WavefrontTuning& t, cudaStream_t s) {
+                                 int npass, int iterations, const WavefrontTuning& t, cudaStream_t s,
+                                 StageTimer* timer) {
     const WfView v = view_of(wb);
     const int n = W.w * W.h * npass;
     const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
-    wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, first_pass, npass);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = timed(timer, STAGE_GENERATE, s, [&] {
+        wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, first_pass, npass);
+        return cudaGetLastError();
+    });
     if (e != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
         const int in = it & 1;
-        wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
-        wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = timed(timer, STAGE_EXTEND, s, [&] {
+                 wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
+                 return cudaGetLastError();
+             })) != cudaSuccess)
+            return e;
+        if ((e = timed(timer, STAGE_SHADE, s,
+                       [&] { return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
+            return e;
+        if ((e = timed(timer, STAGE_SHADOW, s, [&] {
+                 wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris);
+                 return cudaGetLastError();
+             })) != cudaSuccess)
+            return e;
     }
     return cudaSuccess;
 }
 
 cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
-                             bool use_graph, cudaStream_t s) {
+                             bool use_graph, cudaStream_t s, int* launches, StageTimer* timer) {
+    if (timer) use_graph = false;
+    int dummy = 0;
+    int& nl = launches ? *launches : dummy;
+    nl = 0;
     if (W.w <= 0 || W.h <= 0 || W.num_passes <= 0) return cudaSuccess;
     const int npix = W.w * W.h;
     const int per_batch = std::max(1, std::min(W.num_passes, wb.capacity / npix));
@@ -424,7 +527,7 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
         if (use_graph) {
             cudaGraph_t g = nullptr;
             if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-            cudaError_t ce = enqueue_batch(p, W, wb, first, npass, iterations, t, s);
+            cudaError_t ce = enqueue_batch(p, W, wb, first, npass, iterations, t, s, nullptr);
             e = cudaStreamEndCapture(s, &g);
             if (ce != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -451,9 +554,10 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
             }
             cudaGraphDestroy(g);
             if ((e = cudaGraphLaunch(wb.graph_exec, s)) != cudaSuccess) return e;
-        } else if ((e = enqueue_batch(p, W, wb, first, npass, iterations, t, s)) != cudaSuccess) {
+        } else if ((e = enqueue_batch(p, W, wb, first, npass, iterations, t, s, timer)) != cudaSuccess) {
             return e;
         }
+        nl += 1 + 3 * iterations;
         if (may_linger) {
             // bounded host loop over the remaining alpha pass-through paths
             for (int it = iterations, guard = 0; guard < 65536; ++it, ++guard) {
@@ -464,15 +568,20 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
                 if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
                 if (count == 0) break;
                 const int in = it & 1;
-                wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in);
+                wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
                 if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
-                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v);
+                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris);
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                nl += 3;
             }
         }
         const int res_grid = std::min((npix + 255) / 256, t.resident_blocks_256);
-        wf_resolve<<<res_grid, 256, 0, s>>>(p, W, v, npass);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = timed(timer, STAGE_RESOLVE, s, [&] {
+                 wf_resolve<<<res_grid, 256, 0, s>>>(p, W, v, npass);
+                 return cudaGetLastError();
+             })) != cudaSuccess)
+            return e;
+        nl += 1;
     }
     return cudaSuccess;
 }
@@ -492,6 +601,14 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     t.shade_grid = sms * std::max(1, b_shade);
     t.shadow_grid = sms * std::max(1, b_shadow);
     t.resident_blocks_256 = sms * std::max(1, b256);
+    if (const char* r = std::getenv("PT_WAVEFRONT_REFILL")) {
+        const int v = std::atoi(r);
+        if (v >= 1 && v <= 32) t.extend_refill = t.shadow_refill = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_MIN_TRIS")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v <= 32) t.min_tris = v;
+    }
     return cudaSuccess;
 }
 

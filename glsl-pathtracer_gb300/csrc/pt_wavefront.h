@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "pt_params.h"
 
@@ -28,15 +29,38 @@ struct WavefrontBuffers {
 // Block sizes and persistent grid sizes of the stage kernels.
 struct WavefrontTuning {
     int extend_block = 128, shade_block = 128, shadow_block = 128;
+    // idle lanes of a warp that trigger a retire + refill round in the
+    // persistent extend / shadow kernels (PT_WAVEFRONT_REFILL overrides)
+    int extend_refill = 8, shadow_refill = 8;
+    // triangle steps run when at least min_tris lanes of a warp have
+    // triangles pending; fewer are postponed (0: every lane steps on its own;
+    // PT_WAVEFRONT_MIN_TRIS overrides).  Needs trav_postpone_fits(depth).
+    int min_tris = 8;
     int extend_grid = 0, shade_grid = 0, shadow_grid = 0;
     int resident_blocks_256 = 0;
+};
+
+// Per-stage device time (CUDA events recorded around each launch on the
+// launching stream), for profiling runs; batches then run without graphs.
+enum { STAGE_GENERATE = 0, STAGE_EXTEND = 1, STAGE_SHADE = 2, STAGE_SHADOW = 3, STAGE_RESOLVE = 4, STAGE_COUNT = 5 };
+struct StageTimer {
+    std::vector<cudaEvent_t> pool;  // 2 events per recorded launch
+    std::vector<int> kinds;         // stage of each recorded launch
+    size_t used = 0;
+    cudaError_t mark(cudaStream_t s);
+    void reset() { used = 0; kinds.clear(); }
+    // sums per stage (ms, launches); synchronises with the recorded events
+    cudaError_t summarise(float ms[STAGE_COUNT], int launches[STAGE_COUNT]) const;
+    void release();
 };
 
 size_t wavefront_bytes_per_path();
 cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity);
 void wavefront_free(WavefrontBuffers& wb);
 cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block);
+// *launches (if given) receives the number of kernels launched; with a
+// timer, every launch is timed (and no graph is used).
 cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
-                             bool use_graph, cudaStream_t s);
+                             bool use_graph, cudaStream_t s, int* launches = nullptr, StageTimer* timer = nullptr);
 
 }  // namespace ptgb

@@ -73,8 +73,15 @@ class pt_hit(C.Structure):
 class pt_stats(C.Structure):
     _fields_ = [
         ("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
-        ("kernel_ms", C.c_float), ("status", C.c_int32),
+        ("kernel_ms", C.c_float), ("status", C.c_int32), ("kernel_launches", C.c_int32),
     ]
+
+
+class pt_stage_stats(C.Structure):
+    _fields_ = [("ms", C.c_float * 5), ("launches", C.c_int32 * 5)]
+
+
+STAGES = ("generate", "extend", "shade", "shadow", "resolve")
 
 
 # Default RenderOptions (src/core/Renderer.h:39-69)
@@ -151,12 +158,17 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_get_output.argtypes = [P, C.c_int32, C.c_int32, _u8]
     lib.pt_trace_rays.argtypes = [P, C.POINTER(pt_ray), C.c_int32, C.POINTER(pt_hit)]
     lib.pt_trace_shadow.argtypes = [P, C.POINTER(pt_ray), _f, C.c_int32, _u8]
+    lib.pt_bsdf_eval.argtypes = [P, _f, _f, _f, _f, C.c_int32, _f, _f]
+    lib.pt_bsdf_sample.argtypes = [P, _f, _f, _f, C.POINTER(C.c_uint32), C.c_int32, _f, _f, _f]
+    lib.pt_set_stage_timing.argtypes = [P, C.c_int32]
+    lib.pt_get_stage_stats.argtypes = [P, C.POINTER(pt_stage_stats)]
     lib.pt_get_stats.argtypes = [P, C.POINTER(pt_stats)]
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in ("pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
-                 "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_passes",
-                 "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
-                 "pt_get_stats", "pt_last_error"):
+                 "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
+                 "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
+                 "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing",
+                 "pt_get_stage_stats", "pt_get_stats", "pt_last_error"):
         getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib
@@ -165,8 +177,9 @@ def load_library(path: str | None = None) -> C.CDLL:
 
 HEADER_SYMBOLS = [
     "pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
-    "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_passes",
-    "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow", "pt_get_stats",
+    "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", 
+    "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
+    "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing", "pt_get_stage_stats", "pt_get_stats",
     "pt_last_error",
 ]
 

@@ -97,7 +97,15 @@ class GpuRenderer:
         s = capi.pt_stats()
         self._ck(self.lib.pt_get_stats(self.ctx, C.byref(s)))
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
-                    status=s.status)
+                    status=s.status, launches=s.kernel_launches)
+
+    def set_stage_timing(self, on: bool):
+        self._ck(self.lib.pt_set_stage_timing(self.ctx, 1 if on else 0))
+
+    def stage_stats(self) -> dict:
+        s = capi.pt_stage_stats()
+        self._ck(self.lib.pt_get_stage_stats(self.ctx, C.byref(s)))
+        return {name: (float(s.ms[k]), int(s.launches[k])) for k, name in enumerate(capi.STAGES)}
 
     def update_instances(self, transforms, materials, tlas_nodes):
         t = np.ascontiguousarray(transforms, np.float32)

@@ -139,6 +139,7 @@ typedef struct pt_stats {
     uint64_t paths;                  /* camera paths traced */
     float    kernel_ms;              /* device time of the last render call (CUDA events) */
     int32_t  status;                 /* device status word of the last call (PT_OK or PT_ERR_*) */
+    int32_t  kernel_launches;        /* kernels the last render call launched */
 } pt_stats;
 
 #define PT_INTEGRATOR_MEGAKERNEL 0
@@ -224,6 +225,33 @@ int pt_trace_rays(pt_context* ctx, const pt_ray* rays, int32_t n, pt_hit* hits);
  * per-ray max distances; occluded[i] = 1 if something is hit before max_dist[i]. */
 int pt_trace_shadow(pt_context* ctx, const pt_ray* rays, const float* max_dist,
                     int32_t n, uint8_t* occluded);
+
+/* Test hook: DisneyEval (disney.glsl:244-351) on n explicit inputs.
+ * records: 20 floats each -- baseColor xyz, metallic, roughness, subsurface,
+ * specularTint, sheen, sheenTint, clearcoat, clearcoatRoughness, specTrans,
+ * ior, ax, ay, eta, anisotropic, 3 unused (the material as GetMaterial
+ * leaves it, pathtrace.glsl:25-115); V, N, L: 3 floats each.  Outputs f
+ * (3 floats, f * |cos L|) and pdf per input. */
+int pt_bsdf_eval(pt_context* ctx, const float* records, const float* V, const float* N, const float* L,
+                 int32_t n, float* f, float* pdf);
+
+/* Test hook: DisneySample (disney.glsl:142-242) with the RNG state given per
+ * input (4 uint32: the PCG4D seed, globals.glsl:149-166).  Outputs the
+ * sampled L, f and pdf. */
+int pt_bsdf_sample(pt_context* ctx, const float* records, const float* V, const float* N,
+                   const uint32_t* seeds, int32_t n, float* L, float* f, float* pdf);
+
+/* Per-stage device time of the wavefront integrator (no counterpart in the
+ * reference; a profiling aid).  With stage timing on, each wavefront launch
+ * of a render call is bracketed by CUDA events on the context's stream and
+ * batches run without CUDA graphs. */
+typedef struct pt_stage_stats {
+    float   ms[5];        /* generate, extend, shade, shadow, resolve: summed device time */
+    int32_t launches[5];  /* launches of each stage */
+} pt_stage_stats;
+int pt_set_stage_timing(pt_context* ctx, int32_t on);
+/* Stage times of the last render call (synchronises with its events). */
+int pt_get_stage_stats(pt_context* ctx, pt_stage_stats* stats);
 
 /* Counters and device time of the last pt_render_* call. */
 int pt_get_stats(pt_context* ctx, pt_stats* stats);

@@ -21,9 +21,10 @@ template <class R> int render_impl(const pt_scene_desc* d, const pt_render_optio
     if (row_step < 1) row_step = 1;
     if (nthreads > 0) omp_set_num_threads(nthreads);
     uint64_t c_closest = 0, c_shadow = 0, c_nodes = 0, c_tris = 0, c_overflow = 0, c_paths = 0, c_hits = 0;
+    uint64_t c_nodes_any = 0, c_tris_any = 0;
     std::vector<int> rows;
     for (int y = row_start; y < H; y += row_step) rows.push_back(y);
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : c_closest, c_shadow, c_nodes, c_tris, c_overflow, c_paths, c_hits)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : c_closest, c_shadow, c_nodes, c_tris, c_overflow, c_paths, c_hits, c_nodes_any, c_tris_any)
     for (int ri = 0; ri < (int)rows.size(); ++ri) {
         const int py = rows[ri];
         Counters cnt;
@@ -51,10 +52,12 @@ template <class R> int render_impl(const pt_scene_desc* d, const pt_render_optio
         }
         c_closest += cnt.closest; c_shadow += cnt.shadow; c_nodes += cnt.nodes; c_tris += cnt.tris;
         c_overflow += cnt.overflow; c_hits += cnt.tri_hits;
+        c_nodes_any += cnt.nodes_any; c_tris_any += cnt.tris_any;
     }
     if (counters) {
         counters[0] = c_closest; counters[1] = c_shadow; counters[2] = c_nodes;
         counters[3] = c_tris; counters[4] = c_overflow; counters[5] = c_paths; counters[6] = c_hits;
+        counters[7] = c_nodes_any; counters[8] = c_tris_any;
     }
     return 0;
 }
@@ -166,8 +169,10 @@ extern "C" {
 // Renders sample passes [first_pass, first_pass+num_passes) of rows
 // row_start, row_start+row_step, ... and ADDS them into accum (W*H*4 floats;
 // RGB radiance + alpha) and accum_sq (W*H*3, sum of squares; may be NULL).
-// counters (6 x uint64): closest-hit queries, shadow queries, node visits,
-// triangle tests, stack overflows, paths.
+// counters (9 x uint64): closest-hit queries, shadow queries, node visits,
+// triangle tests, stack overflows, paths, triangle hits of closest-hit
+// queries, and the node visits and triangle tests of the any-hit queries
+// alone (already included in the totals).
 // cull = 1 counts node visits / triangle tests of a tmax-culled traversal
 // (same hits; the work counts define the roofline's bytes per ray).
 int orc_render(const pt_scene_desc* d, const pt_render_options* o, const pt_camera* cam, int first_pass,

@@ -290,6 +290,7 @@ template <class R> struct Light { V3<R> position, emission, u, v; R radius, area
 // Counters of executed ray queries and traversal work.
 struct Counters {
     uint64_t closest = 0, shadow = 0, nodes = 0, tris = 0, overflow = 0, tri_hits = 0;
+    uint64_t nodes_any = 0, tris_any = 0;  // the part of nodes / tris done by any-hit queries
 };
 
 // ------------------------------------------------------------ textures
@@ -595,6 +596,7 @@ template <class R> inline bool AnyHit(const Scene<R>& s, const Ray<R>& r, R maxD
         int leftIndex, rightIndex, leaf;
         s.node_lrl(index, leftIndex, rightIndex, leaf);
         cnt.nodes++;
+        cnt.nodes_any++;
         if (leaf > 0) {
             for (int i = 0; i < rightIndex; i++) {
                 const int32_t* vi = s.d->vert_indices + 3 * (size_t)(leftIndex + i);
@@ -602,6 +604,7 @@ template <class R> inline bool AnyHit(const Scene<R>& s, const Ray<R>& r, R maxD
                 V3<R> v0 = s.vtx(vi[0], w0), v1 = s.vtx(vi[1], w1), v2 = s.vtx(vi[2], w2);
                 R u, v, tt, w;
                 cnt.tris++;
+                cnt.tris_any++;
                 if (TriTest(rTrans.origin, rTrans.direction, v0, v1, v2, u, v, tt, w) && tt < maxDist) {
                     if (!alpha) return true;
                     R n0w, n1w, n2w;
