@@ -499,6 +499,56 @@ int pt_render_tile(pt_context* c, int32_t tx, int32_t ty, int32_t frame) {
     return render(c, w);
 }
 
+// One tile with the wavefront integrator, its path state in the fixed device
+// array of pt_wavefront.cu instead of the context's cudaMalloc'd batch: the
+// tile runs in bands of whole rows of at most kFixedScratchPaths pixels.
+// Path seeds depend only on the pixel and the tile, so the bands give the
+// samples pt_render_tile gives.  No CUDA graph is built (instantiating one
+// allocates).
+int pt_render_tile_noalloc(pt_context* c, int32_t tx, int32_t ty, int32_t frame) {
+    if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
+    const pt_render_options& o = c->opts;
+    const int ntx = (o.render_width + o.tile_width - 1) / o.tile_width;
+    const int nty = (o.render_height + o.tile_height - 1) / o.tile_height;
+    if (tx < 0 || ty < 0 || tx >= ntx || ty >= nty) return set_err(PT_ERR_INVALID_ARG, "tile out of range");
+    if (frame < 0) return set_err(PT_ERR_INVALID_ARG, "negative frame number");
+    RenderWork w;
+    w.x0 = tx * o.tile_width;
+    w.y0 = ty * o.tile_height;
+    w.w = std::min(o.tile_width, o.render_width - w.x0);
+    w.h = std::min(o.tile_height, o.render_height - w.y0);
+    w.first_pass = 0;
+    w.num_passes = 1;
+    w.tile_frame = frame;
+    w.tile_x = tx;
+    w.tile_y = ty;
+    if (w.w > kFixedScratchPaths)
+        return set_err(PT_ERR_INVALID_ARG, "pt_render_tile_noalloc: tile rows of more than 16384 pixels do not fit "
+                                           "the fixed path-state scratch");
+    WavefrontBuffers wb;
+    CK(wavefront_fixed_buffers(wb));
+    if (!c->wf_tuned) {
+        CK(wavefront_default_tuning(c->wf_tuning, 128));
+        c->wf_tuned = true;
+    }
+    if (int rc = begin_launch(c)) return rc;
+    const Params p = make_params(c);
+    const int rows = kFixedScratchPaths / w.w;
+    int launches = 0;
+    for (int y = 0; y < w.h; y += rows) {
+        RenderWork band = w;
+        band.y0 = w.y0 + y;
+        band.h = std::min(rows, w.h - y);
+        int n = 0;
+        WavefrontTuning t = c->wf_tuning;
+        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+        CK(launch_wavefront(p, band, wb, t, false, c->stream, &n));
+        launches += n;
+    }
+    c->launches = launches;
+    return end_launch(c);
+}
+
 int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {
     if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
     if (first_pass < 0 || num_passes < 0) return set_err(PT_ERR_INVALID_ARG, "negative pass range");

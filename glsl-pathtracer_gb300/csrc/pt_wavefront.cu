@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdlib>
 
 #include "../../include/pt_cuda.h"
@@ -430,6 +431,57 @@ void wavefront_free(WavefrontBuffers& wb) {
         if (p) cudaFree(p);
     if (wb.graph_exec) cudaGraphExecDestroy(wb.graph_exec);
     wb = WavefrontBuffers{};
+}
+
+// Fixed scratch: 17 float4-sized arrays and 3 int arrays of
+// kFixedScratchPaths entries, then 8 counters, each array 256-byte aligned
+// (4.4 MiB).  Nothing in it needs to start at zero: each batch's first
+// kernel (wf_generate) writes the counters and queue entries it reads.
+namespace {
+constexpr size_t kFixedVec = (size_t)kFixedScratchPaths * 16;
+constexpr size_t kFixedInt = (size_t)kFixedScratchPaths * 4;
+constexpr size_t kFixedBytes = 17 * kFixedVec + 3 * kFixedInt + 256;
+static_assert(kFixedVec % 256 == 0 && kFixedInt % 256 == 0, "scratch arrays stay 256-byte aligned");
+constexpr int kFixedMaxDevices = 64;
+std::atomic<char*> g_fixed_addr[kFixedMaxDevices];
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_fixed_scratch[kFixedBytes];
+
+cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kFixedMaxDevices) return cudaErrorInvalidDevice;
+    char* base = g_fixed_addr[dev].load(std::memory_order_acquire);
+    if (!base) {
+        void* addr = nullptr;
+        if ((e = cudaGetSymbolAddress(&addr, g_fixed_scratch)) != cudaSuccess) return e;
+        base = static_cast<char*>(addr);
+        g_fixed_addr[dev].store(base, std::memory_order_release);
+    }
+    wb = WavefrontBuffers{};
+    wb.capacity = kFixedScratchPaths;
+    float4** f4[] = {&wb.o, &wb.d, &wb.T, &wb.L, &wb.med, &wb.h0, &wb.h2, &wb.so, &wb.sd0, &wb.sd1,
+                     &wb.sc0, &wb.sc1, &wb.sT, &wb.rad};
+    size_t off = 0;
+    for (float4** q : f4) {
+        *q = reinterpret_cast<float4*>(base + off);
+        off += kFixedVec;
+    }
+    wb.rng = reinterpret_cast<uint4*>(base + off);
+    off += kFixedVec;
+    wb.misc = reinterpret_cast<int4*>(base + off);
+    off += kFixedVec;
+    wb.h1 = reinterpret_cast<int4*>(base + off);
+    off += kFixedVec;
+    int** i1[] = {&wb.q[0], &wb.q[1], &wb.qs};
+    for (int** q : i1) {
+        *q = reinterpret_cast<int*>(base + off);
+        off += kFixedInt;
+    }
+    wb.counts = reinterpret_cast<int*>(base + off);
+    return cudaSuccess;
 }
 
 cudaError_t StageTimer::mark(cudaStream_t s) {

@@ -55,6 +55,13 @@ struct StageTimer {
 };
 
 size_t wavefront_bytes_per_path();
+// Path state in a fixed device array of kFixedScratchPaths paths instead of
+// cudaMalloc'd buffers (pt_render_tile_noalloc).  The first call on a device
+// looks the array's address up (cudaGetSymbolAddress, with that device
+// current); later calls only carve it.  Every context on the device shares
+// the one array, so its users must not overlap in time.
+constexpr int kFixedScratchPaths = 16384;
+cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb);
 cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity);
 void wavefront_free(WavefrontBuffers& wb);
 cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block);

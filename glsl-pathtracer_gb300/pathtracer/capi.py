@@ -152,6 +152,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_update_envmap.argtypes = [P, _f, _f, C.c_int32, C.c_int32, C.c_float]
     lib.pt_clear_accum.argtypes = [P]
     lib.pt_render_tile.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
+    lib.pt_render_tile_noalloc.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.pt_render_passes.argtypes = [P, C.c_int32, C.c_int32]
     lib.pt_get_accum.argtypes = [P, _f]
     lib.pt_snapshot_accum.argtypes = [P]
@@ -166,7 +167,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in ("pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
-                 "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
+                 "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
                  "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing",
                  "pt_get_stage_stats", "pt_get_stats", "pt_last_error"):
         getattr(lib, name).restype = C.c_int
@@ -177,7 +178,7 @@ def load_library(path: str | None = None) -> C.CDLL:
 
 HEADER_SYMBOLS = [
     "pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
-    "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", 
+    "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_tile_noalloc",
     "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
     "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing", "pt_get_stage_stats", "pt_get_stats",
     "pt_last_error",

@@ -194,6 +194,22 @@ int pt_clear_accum(pt_context* ctx);
  * frame number frame_num and adds it to the accumulation buffer. */
 int pt_render_tile(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t frame_num);
 
+/* No counterpart in the reference.  pt_render_tile with the wavefront
+ * integrator, for callers that must not allocate device memory while they
+ * render (code running inside a memory budget fixed up front, or between
+ * calls that must not synchronise the device, as cudaMalloc/cudaFree can):
+ * the path state lives in one fixed device array of 16384 paths (4.4 MiB,
+ * part of the loaded library), and tiles are traced in bands of whole rows
+ * of at most 16384 pixels, giving the samples pt_render_tile gives.  The
+ * first call on a device does a one-time set-up (looks the array up); make
+ * that call before any stream capture.  Tiles wider than 16384 pixels are
+ * rejected with PT_ERR_INVALID_ARG.  The array is shared by every context on
+ * the device: calls that overlap in time (other streams, threads or
+ * contexts) race on it and must be serialised by the caller.  Nothing in it
+ * needs to start at zero.  The context's accumulation buffer is the one
+ * pt_render_tile adds to (clear it with pt_clear_accum). */
+int pt_render_tile_noalloc(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t frame_num);
+
 /* Whole-frame form of the same work: sample passes first_pass ..
  * first_pass+num_passes-1, each pass being every tile in the reference's
  * order (Renderer.cpp:745-762), with the frame numbers the tile state machine
