@@ -13,10 +13,18 @@ segments), counted on the device.
   e2e        through the public C ABI with host buffers, wall clock per step:
              pt_set_camera + pt_render_passes + pt_get_output (tonemapped
              RGBA8 image copied to pinned host memory).
-  roofline   HBM: algorithmic bytes per ray (36 B per node visit + 60 B per
-             triangle test + 176 B per triangle hit, counted by the oracle with
-             a tmax-culled traversal of the reference's binary BVH on a row
-             sample) x rays per launch / kernel time, against MEASURED_PEAKS.json.
+  compare    the megakernel on the same frame and timing rules (it gives the
+             same accumulation bit for bit, so equal RMSE): the
+             wavefront / megakernel ratio.
+  roofline   HBM, for the dominant kernel (wf_extend on this workload): its
+             algorithmic bytes (36 B per node visit + 60 B per triangle test
+             + 176 B per triangle hit of a closest-hit query, counted by the
+             oracle with a tmax-culled traversal of the reference's binary
+             BVH on a row sample) x the queries of its launches / its own
+             launch durations, taken with CUDA events around every launch on
+             the launching stream in --stage-steps extra frames; against
+             MEASURED_PEAKS.json.  traffic: DRAM bytes per launch from the
+             ncu capture in profiles/, scaled by the launch's queries.
   cpu_baseline  the oracle (C++ restatement of the reference's shaders, the
              reference's traversal, FP32, OpenMP on all host cores) on a row
              sample of the same frame.
@@ -127,15 +135,27 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes per closest-hit query of wf_extend on the icosphere workload:
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch / its rays, from
+# profiles/wf_extend_wf_shadow_icosphere_1m_1spp.md (traffic grows with the
+# rays of a launch: path-state reads and writes, BVH misses in L2).
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 95.3}
+
+
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
     """Oracle work counts (tmax-culled traversal of the reference's binary
-    BVH) on a row sample -> algorithmic bytes per ray query."""
+    BVH) on a row sample -> algorithmic bytes per ray query: all queries,
+    closest-hit queries alone and any-hit queries alone."""
     import orc
     _, _, c = orc.render(scene, options, camera, 0, passes, row_step=row_step, cull=True)
     rays = c["closest"] + c["shadow"]
     b = (36.0 * c["nodes"] + 60.0 * c["tris"] + 176.0 * c["tri_hits"]) / max(rays, 1)
+    nc, tc = c["nodes"] - c["nodes_any"], c["tris"] - c["tris_any"]
+    b_closest = (36.0 * nc + 60.0 * tc + 176.0 * c["tri_hits"]) / max(c["closest"], 1)
+    b_shadow = (36.0 * c["nodes_any"] + 60.0 * c["tris_any"]) / max(c["shadow"], 1)
     return b, dict(nodes_per_ray=c["nodes"] / rays, tris_per_ray=c["tris"] / rays,
-                   hits_per_ray=c["tri_hits"] / rays, rays=rays)
+                   hits_per_ray=c["tri_hits"] / rays, rays=rays, bytes_per_closest_ray=b_closest,
+                   bytes_per_shadow_ray=b_shadow)
 
 
 def cpu_baseline(scene, options, camera, spp, target_s=15.0):
@@ -207,6 +227,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=3,
                     help="timed steps of the other integrator, for the wavefront/megakernel ratio (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage-steps", type=int, default=3,
+                    help="extra steps timed per kernel with CUDA events (roofline of the dominant kernel)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
     ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
     args = ap.parse_args()
@@ -307,6 +329,28 @@ def main():
                  "wavefront_over_megakernel": (value / o_val) if other_name == "megakernel" else (o_val / value)}
         r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else capi.PT_INTEGRATOR_MEGAKERNEL)
 
+    # per-kernel device time: the same frames again with CUDA events around
+    # every launch (no graph), for the roofline of the dominant kernel
+    stages = None
+    if args.integrator == "wavefront" and args.stage_steps > 0:
+        r.set_stage_timing(True)
+        tot = {k: [0.0, 0] for k in capi.STAGES}
+        st_rays = {"closest": 0, "shadow": 0}
+        base3 = pass_base + (args.warmup + 3 * args.steps + 8) * spp
+        for k in range(args.stage_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                r.render_passes(base3 + k * spp, spp)
+            st = r.stats()
+            st_rays["closest"] += st["closest"]
+            st_rays["shadow"] += st["shadow"]
+            for name, (ms_k, n_k) in r.stage_stats().items():
+                tot[name][0] += ms_k
+                tot[name][1] += n_k
+        r.set_stage_timing(False)
+        stages = {"ms": {k: v[0] for k, v in tot.items()}, "launches": {k: v[1] for k, v in tot.items()},
+                  "rays": st_rays, "steps": args.stage_steps}
+
     # end to end through the C ABI with host buffers
     import ctypes as C
     lib = capi.load_library()
@@ -333,13 +377,31 @@ def main():
         b_ray, work = bytes_per_ray(sd, sd.render_options(), cam)
         mean_ms = statistics.mean(ms)
         achieved = b_ray * rays_per_step / (mean_ms / 1000.0) / 1e9
-        traffic = None
-        tfile = os.path.join(ROOT, "profiles", "traffic_per_ray.json")
-        if os.path.exists(tfile):
-            with open(tfile) as fh:
-                tp = json.load(fh)
-            if tp.get("config") == args.config and tp.get("integrator") == args.integrator:
-                traffic = tp["dram_bytes_per_ray"] * rays_per_step
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                    "kernel": "whole frame", "bytes_per_ray": b_ray, **work}
+        if stages:
+            # the dominant kernel: algorithmic bytes of its queries / its own
+            # event-timed launch durations
+            per = {"extend": ("wf_extend", stages["rays"]["closest"], work["bytes_per_closest_ray"]),
+                   "shadow": ("wf_shadow", stages["rays"]["shadow"], work["bytes_per_shadow_ray"])}
+            kernels = {}
+            for key, (kname, nrays, bpr) in per.items():
+                kms, nl = stages["ms"][key], max(stages["launches"][key], 1)
+                a = bpr * nrays / (kms / 1000.0) / 1e9
+                kernels[kname] = {"achieved": a, "frac": a / peak, "avg_launch_ms": kms / nl, "launches": nl,
+                                  "rays_per_launch": nrays / nl, "bytes_per_ray": bpr,
+                                  "share_of_frame": kms / max(sum(stages["ms"].values()), 1e-9)}
+            dom = max(kernels, key=lambda k: kernels[k]["share_of_frame"])
+            kd = kernels[dom]
+            traffic = None
+            if dom == "wf_extend" and args.config in EXTEND_DRAM_BYTES_PER_RAY and not args.small:
+                traffic = EXTEND_DRAM_BYTES_PER_RAY[args.config] * kd["rays_per_launch"]
+            roofline = {"bound": "hbm", "kernel": dom, "achieved": kd["achieved"], "peak": peak, "unit": "GB/s",
+                        "frac": kd["achieved"] / peak, "traffic": traffic,
+                        "algorithmic_bytes_per_launch": kd["bytes_per_ray"] * kd["rays_per_launch"],
+                        "peak_source": peak_kind, "kernels": kernels,
+                        "frame": {"achieved": achieved, "frac": achieved / peak, "bytes_per_ray": b_ray}, **work}
         cpu = None
         if not args.no_cpu_baseline:
             cpu, _, _ = cpu_baseline(sd, sd.render_options(), cam, spp)
@@ -352,9 +414,7 @@ def main():
                        "l2": "flushed before each timed step (512 MiB write)",
                        "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU"},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "bytes_per_ray": b_ray, **work},
+            "roofline": roofline,
             "e2e": e2e,
             "clocks": clk.summary(),
         }

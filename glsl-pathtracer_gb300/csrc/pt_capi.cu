@@ -15,6 +15,7 @@
 #include "bvh8.h"
 #include "pt_device.cuh"
 #include "pt_params.h"
+#include "pt_grad.cuh"
 #include "pt_wavefront.h"
 
 using namespace ptgb;
@@ -101,6 +102,17 @@ struct pt_context {
     int launches = 0;  // kernels launched by the last render call
     bool stage_timing = false;
     StageTimer timer;
+    // scene / camera / options version, and the forward wavefront batch the
+    // path buffers hold (the adjoint reuses its per-path radiance)
+    uint64_t version = 1;
+    struct {
+        bool valid = false;
+        RenderWork w{};
+        uint64_t version = 0;
+    } fwd;
+    // adjoint buffers
+    DevBuf<float4> adj_v, adj_le;
+    DevBuf<float> adj_dimage, adj_grad;
 };
 
 namespace {
@@ -181,6 +193,22 @@ int check_tlas_materials(const float* tlas_nodes, int n, int num_materials) {
         if (p[8] < 0.0f && (p[7] < 0.0f || p[7] >= (float)num_materials))
             return set_err(PT_ERR_INVALID_ARG, "TLAS leaf material index out of range");
     }
+    return PT_OK;
+}
+
+// Lights repacked as 4 float4 (pt_device.cuh LoadLight) from GLSLPT::Light's
+// 15 floats: position, emission, u, v, radius, area, type (Scene.h:50-59).
+int upload_lights(pt_context* c, const float* lights, int n) {
+    std::vector<float4> L(4 * (size_t)std::max(1, n));
+    for (int i = 0; i < n; ++i) {
+        const float* s = lights + 15 * (size_t)i;
+        L[4 * i + 0] = make_float4(s[0], s[1], s[2], s[12]);
+        L[4 * i + 1] = make_float4(s[3], s[4], s[5], s[13]);
+        L[4 * i + 2] = make_float4(s[6], s[7], s[8], s[14]);
+        L[4 * i + 3] = make_float4(s[9], s[10], s[11], 0.0f);
+    }
+    CK(c->lights.upload(L.data(), L.size(), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return PT_OK;
 }
 
@@ -291,8 +319,15 @@ int render(pt_context* c, const RenderWork& w) {
         WavefrontTuning t = c->wf_tuning;
         if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
         c->timer.reset();
+        c->fwd.valid = false;
         CK(launch_wavefront(p, w, c->wf, t, use_graph, c->stream, &c->launches,
                             c->stage_timing ? &c->timer : nullptr));
+        // one batch: the path buffers keep every path of this work
+        if (!(p.flags & F_ALPHA_TEST) && (long)w.w * w.h * w.num_passes <= c->wf.capacity) {
+            c->fwd.valid = true;
+            c->fwd.w = w;
+            c->fwd.version = c->version;
+        }
     } else {
         CK(launch_render(p, w, c->integrator, c->stream));
         c->launches = 1;
@@ -362,15 +397,7 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
             rc = cuda_err(e, "scene upload");
             break;
         }
-        std::vector<float4> L(4 * (size_t)std::max(1, d->num_lights));
-        for (int i = 0; i < d->num_lights; ++i) {
-            const float* s = d->lights + 15 * (size_t)i;  // position, emission, u, v, (radius, area, type)
-            L[4 * i + 0] = make_float4(s[0], s[1], s[2], s[12]);
-            L[4 * i + 1] = make_float4(s[3], s[4], s[5], s[13]);
-            L[4 * i + 2] = make_float4(s[6], s[7], s[8], s[14]);
-            L[4 * i + 3] = make_float4(s[9], s[10], s[11], 0.0f);
-        }
-        if ((e = c->lights.upload(L.data(), L.size(), c->stream)) != cudaSuccess) { rc = cuda_err(e, "lights"); break; }
+        if ((rc = upload_lights(c, d->lights, d->num_lights))) break;
         if ((rc = upload_envmap(c, d->envmap_rgb, d->envmap_cdf, d->envmap_width, d->envmap_height,
                                 d->envmap_total_sum)))
             break;
@@ -415,6 +442,7 @@ int pt_set_stream(pt_context* c, void* s) {
 int pt_set_camera(pt_context* c, const pt_camera* cam) {
     if (!c || !cam) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     c->cam = *cam;
+    c->version++;
     return PT_OK;
 }
 
@@ -424,6 +452,7 @@ int pt_set_options(pt_context* c, const pt_render_options* o) {
     const bool resize = o->render_width != c->opts.render_width || o->render_height != c->opts.render_height ||
                         o->tile_width != c->opts.tile_width || o->tile_height != c->opts.tile_height;
     c->opts = *o;
+    c->version++;
     if (resize) return alloc_accum(c);
     return PT_OK;
 }
@@ -444,6 +473,7 @@ int pt_update_instances(pt_context* c, const float* transforms, int32_t num_inst
         if (num_materials <= 0) return set_err(PT_ERR_INVALID_ARG, "num_materials must be positive");
         if (int rc = check_materials(materials, num_materials)) return rc;
     }
+    c->version++;
     int rc = check_tlas_materials(tlas_nodes, num_tlas_nodes, materials ? num_materials : c->num_materials);
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
@@ -470,6 +500,7 @@ int pt_update_envmap(pt_context* c, const float* rgb, const float* cdf, int32_t 
     if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
     if (rgb && (w <= 0 || h <= 0 || !cdf)) return set_err(PT_ERR_INVALID_ARG, "invalid envmap");
     CK(cudaStreamSynchronize(c->stream));
+    c->version++;
     return upload_envmap(c, rgb, cdf, w, h, total);
 }
 
@@ -547,6 +578,96 @@ int pt_render_tile_noalloc(pt_context* c, int32_t tx, int32_t ty, int32_t frame)
     }
     c->launches = launches;
     return end_launch(c);
+}
+
+int pt_update_materials(pt_context* c, const float* materials, int32_t num_materials) {
+    if (!c || !materials) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (num_materials != c->num_materials)
+        return set_err(PT_ERR_INVALID_ARG, "pt_update_materials: the number of materials cannot change");
+    if (int rc = check_materials(materials, num_materials)) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(c->mats.upload(materials, 8 * (size_t)num_materials, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->scene_flags = scene_flags_of(materials, num_materials, c->num_lights);
+    c->version++;
+    return PT_OK;
+}
+
+int pt_update_lights(pt_context* c, const float* lights, int32_t num_lights) {
+    if (!c || (num_lights > 0 && !lights)) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (num_lights != c->num_lights)
+        return set_err(PT_ERR_INVALID_ARG, "pt_update_lights: the number of lights cannot change");
+    for (int i = 0; i < num_lights; ++i) {
+        const int type = (int)lights[15 * i + 14];
+        if (type < 0 || type > 2) return set_err(PT_ERR_INVALID_ARG, "unknown light type");
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (int rc = upload_lights(c, lights, num_lights)) return rc;
+    c->version++;
+    return PT_OK;
+}
+
+int pt_render_adjoint(pt_context* c, int32_t first_pass, int32_t num_passes, const float* d_image, float* grad) {
+    if (!c || !d_image || !grad) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (first_pass < 0 || num_passes <= 0) return set_err(PT_ERR_INVALID_ARG, "invalid pass range");
+    const uint32_t flags = option_flags(c);
+    if (flags & (F_MEDIUM | F_ALPHA_TEST | F_ENVMAP))
+        return set_err(PT_ERR_UNSUPPORTED,
+                       "pt_render_adjoint: media, alpha-tested materials and environment maps are not differentiated");
+    RenderWork w;
+    w.x0 = w.y0 = 0;
+    w.w = c->opts.render_width;
+    w.h = c->opts.render_height;
+    w.first_pass = first_pass;
+    w.num_passes = num_passes;
+    w.tile_frame = -1;
+    w.tile_x = w.tile_y = 0;
+    const long paths = (long)w.w * w.h * num_passes;
+    if (paths > (1L << 26)) return set_err(PT_ERR_UNSUPPORTED, "pt_render_adjoint: more than 2^26 paths in one call");
+    if (c->wf.capacity < paths) {
+        CK(wavefront_alloc(c->wf, (int)paths));
+        c->fwd.valid = false;
+    }
+    if (!c->wf_tuned) {
+        CK(wavefront_default_tuning(c->wf_tuning, 128));
+        c->wf_tuned = true;
+    }
+    if ((long)c->adj_le.n < c->wf.capacity) {
+        CK(c->adj_v.alloc(3 * (size_t)c->wf.capacity));
+        CK(c->adj_le.alloc((size_t)c->wf.capacity));
+    }
+    const int gsize = c->num_materials * grad::kParams + 3 * c->num_lights;
+    const size_t npix_full = (size_t)c->opts.render_width * c->opts.render_height;
+    CK(c->adj_dimage.upload(d_image, 3 * npix_full, c->stream));
+    if ((int)c->adj_grad.n != gsize) CK(c->adj_grad.alloc(gsize));
+    CK(cudaMemsetAsync(c->adj_grad.p, 0, sizeof(float) * gsize, c->stream));
+    AdjView A;
+    A.dimage = c->adj_dimage.p;
+    A.inv_passes = 1.0f / (float)num_passes;
+    A.width = c->opts.render_width;
+    A.grad = c->adj_grad.p;
+    A.num_materials = c->num_materials;
+    A.num_lights = c->num_lights;
+    A.grad_size = gsize;
+    A.shared = gsize <= 8192;  // up to 32 KB of shared memory per block
+    A.v = c->adj_v.p;
+    A.le = c->adj_le.p;
+    const bool cached = c->fwd.valid && c->fwd.version == c->version && c->fwd.w.x0 == w.x0 &&
+                        c->fwd.w.y0 == w.y0 && c->fwd.w.w == w.w && c->fwd.w.h == w.h &&
+                        c->fwd.w.first_pass == w.first_pass && c->fwd.w.num_passes == w.num_passes &&
+                        c->fwd.w.tile_frame == w.tile_frame;
+    if (int rc = begin_launch(c)) return rc;
+    WavefrontTuning t = c->wf_tuning;
+    if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+    CK(launch_adjoint(make_params(c), w, c->wf, t, A, !cached, c->stream, &c->launches));
+    if (int rc = end_launch(c)) return rc;
+    c->fwd.valid = false;  // the replay leaves the forward state of the paths, but not in a reusable form
+    CK(cudaMemcpyAsync(grad, c->adj_grad.p, sizeof(float) * gsize, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int st = 0;
+    CK(cudaMemcpy(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) return set_err(st, "pt_render_adjoint: kernel status " + std::to_string(st));
+    return PT_OK;
 }
 
 int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {

@@ -39,6 +39,7 @@ struct HitRecord {
     int prim, inst, mat;
     float lightPdf;
     V3 lightEmission;
+    int light;  // index of the light hit (isEmitter)
 };
 
 struct ShadowReq {
@@ -79,6 +80,7 @@ __device__ __forceinline__ float LightsClosest(const Params& P, const Ray& r, in
                     hr.lightPdf = (t * t) / (L.area * cosTheta);
                     hr.lightEmission = L.emission;
                     hr.isEmitter = true;
+                    hr.light = i;
                 }
             }
             if (type == SPHERE_LIGHT) {
@@ -91,6 +93,7 @@ __device__ __forceinline__ float LightsClosest(const Params& P, const Ray& r, in
                     hr.lightPdf = (t * t) / (L.area * cosTheta * 0.5f);
                     hr.lightEmission = L.emission;
                     hr.isEmitter = true;
+                    hr.light = i;
                 }
             }
         }
@@ -339,10 +342,10 @@ __device__ __forceinline__ V3 ScatterEval(bool isSurface, const Material& mat, f
 // pathtrace.glsl:158-283.  INLINE: shadow rays traced here and the result
 // returned; otherwise the rays and their contributions go to `sr` and the
 // caller adds the unoccluded ones (same values, same order).
-template <int MEDIUM, bool ENV, bool INLINE>
+template <int MEDIUM, bool ENV, bool INLINE, class Hook>
 __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp, V3 normal, V3 ffnormal,
                                           const Material& mat, float eta, const Medium& medium, bool isSurface,
-                                          Rng& rng, uint2* stack, Counters& cnt, ShadowReq& sr) {
+                                          Rng& rng, uint2* stack, Counters& cnt, ShadowReq& sr, Hook& hook) {
     V3 Ld = v3(0.0f);
     V3 Li = v3(0.0f);
     const V3 scatterPos = fhp + normal * PT_EPS;
@@ -423,6 +426,7 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
                     if (sfPdf > 0.0f) {
                         c = misWeight * Li * sf / ls.pdf;
                         adds = true;
+                        hook.nee_light(index, misWeight, Li, sf, ls.pdf, eta, V, ffnormal, ls.direction);
                     }
                 };
                 if (INLINE) {
@@ -458,14 +462,25 @@ __device__ __forceinline__ V3 ResolveShadow(const ShadowReq& sr, bool occ_env, b
     return Ld;
 }
 
+// Observer of the terms of a path that depend on differentiable parameters
+// (the adjoint pass, pt_adjoint.cu).  The forward passes use NoHook, whose
+// empty members compile away.
+struct NoHook {
+    __device__ __forceinline__ void material(const PathState&, float) {}
+    __device__ __forceinline__ void emitter(const PathState&, float, const HitRecord&) {}
+    __device__ __forceinline__ void vertex(const PathState&) {}
+    __device__ __forceinline__ void nee_light(int, float, V3, V3, float, float, V3, V3, V3) {}
+    __device__ __forceinline__ void sample(float, V3, V3, V3, V3, const PathState&, const ShadowReq&) {}
+};
+
 // One iteration of PathTrace's loop (pathtrace.glsl:301-473) for the hit in
 // `hr`.  Returns true if the path continues with ps.r (depth incremented).
 // With INLINE false, a pending next-event estimate is left in `sr`
 // (sr.n != 0): the caller adds ResolveShadow(...) * sr.T to the radiance
 // before anything else touches the path.
-template <int MEDIUM, bool ENV, bool INLINE>
+template <int MEDIUM, bool ENV, bool INLINE, class Hook>
 __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const HitRecord& hr, ShadowReq& sr,
-                                          uint2* stack, Counters& cnt) {
+                                          uint2* stack, Counters& cnt, Hook& hook) {
     const uint32_t F = P.flags;
     sr.n = 0;
     if (!hr.hit) {
@@ -492,6 +507,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
     }
     Material mat;
     float eta;
+    hook.material(ps, ps.prevRough);
     GetMaterial(P, ps.matID, ps.depth, ps.prevRough, normal, ps.r, mat, eta);
     ps.prevRough = mat.roughness;
     ps.radiance = ps.radiance + mat.emission * ps.throughput;
@@ -499,6 +515,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
         float misWeight = 1.0f;
         if (ps.depth > 0) misWeight = PowerHeuristic(ps.scatterPdf, hr.lightPdf);
         if (MEDIUM == 1 && !ps.surfaceScatter) misWeight = 1.0f;
+        hook.emitter(ps, misWeight, hr);
         ps.radiance = ps.radiance + misWeight * hr.lightEmission * ps.throughput;
         return false;
     }
@@ -519,7 +536,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
                     ps.throughput = ps.throughput * ps.medium.color;
                     ps.r.origin = ps.r.origin + ps.r.direction * scatterDist;
                     const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, ps.r.origin, normal, ffnormal, mat, eta,
-                                                                   ps.medium, false, ps.rng, stack, cnt, sr);
+                                                                   ps.medium, false, ps.rng, stack, cnt, sr, hook);
                     if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
                     else sr.T = ps.throughput;
                     float h1 = ps.rng.next();
@@ -537,13 +554,18 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
             ps.depth--;
         } else {
             ps.surfaceScatter = true;
+            hook.vertex(ps);
             const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, fhp, normal, ffnormal, mat, eta, ps.medium, true,
-                                                           ps.rng, stack, cnt, sr);
+                                                           ps.rng, stack, cnt, sr, hook);
             if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
             else sr.T = ps.throughput;
             const V3 f = DisneySample(mat, eta, -ps.r.direction, ffnormal, scatterL, ps.scatterPdf, ps.rng);
-            if (ps.scatterPdf > 0.0f) ps.throughput = ps.throughput * (f / ps.scatterPdf);
-            else return false;
+            if (ps.scatterPdf > 0.0f) {
+                hook.sample(eta, -ps.r.direction, ffnormal, scatterL, f, ps, sr);
+                ps.throughput = ps.throughput * (f / ps.scatterPdf);
+            } else {
+                return false;
+            }
         }
         ps.r.direction = scatterL;
         ps.r.origin = fhp + ps.r.direction * PT_EPS;

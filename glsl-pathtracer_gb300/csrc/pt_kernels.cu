@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(128) render_kernel(Params P, RenderWork W) {
                 HitRecord hr;
                 TraceClosest(P, ps.r, ps.depth, hr, stack, cnt, false);
                 ShadowReq sr;
-                if (!ShadeStep<MEDIUM, ENV, true>(P, ps, hr, sr, stack, cnt)) break;
+                NoHook nh;
+                if (!ShadeStep<MEDIUM, ENV, true>(P, ps, hr, sr, stack, cnt, nh)) break;
             }
             acc.x += ps.radiance.x;
             acc.y += ps.radiance.y;

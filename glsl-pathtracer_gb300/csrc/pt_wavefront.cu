@@ -22,6 +22,7 @@
 #include <cstdlib>
 
 #include "../../include/pt_cuda.h"
+#include "pt_grad.cuh"
 #include "pt_integrator.cuh"
 #include "pt_wavefront.h"
 
@@ -156,7 +157,8 @@ __global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in, 
         if (ray >= 0 && !tracing) {  // retire
             FinishClosest(s, tl, hr);
             B.h0[ray] = make_float4(hr.t, hr.u, hr.v, hr.w);
-            B.h1[ray] = make_int4(hr.prim, hr.inst, hr.mat, (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 : 0));
+            B.h1[ray] = make_int4(hr.prim, hr.inst, hr.mat,
+                                  (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 | (hr.light << 2) : 0));
             B.h2[ray] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
             ray = -1;
         }
@@ -183,9 +185,123 @@ __global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in, 
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
 
-template <int MEDIUM, bool ENV, bool INLINE>
-__global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
+// ------------------------------------------------------------ adjoint
+// Path-replay backpropagation (the adjoint replays each path from its seed,
+// so nothing of the forward pass is kept but each path's radiance L).  The
+// sampling is detached: directions, lobe choices, MIS weights and Russian
+// roulette are held fixed, and the derivative of each term of L is taken
+// through the BSDF values and the light emissions it contains:
+//   - an emitter hit adds w * Le * beta: d/dLe = w * beta;
+//   - next-event estimation adds w * Li * f_L / p * beta, Li = Le * number
+//     of lights: d/dtheta through f_L, d/dLe = w * #lights * f_L / p * beta;
+//     both count only when the shadow ray is unoccluded (wf_shadow);
+//   - every later term is proportional to the BSDF value f of this vertex's
+//     sampled direction, so d/dtheta of (L - terms up to here) is
+//     (L - terms up to here) * df / f per channel.
+// Each term is dotted with dLoss/dL of the path.  The unknown visibility of
+// this vertex's next-event ray at shade time is handled by storing the
+// difference of its two cases for the shadow stage.
+struct AdjHook {
+    const Params* P;
+    const AdjView* A;
+    float* acc;      // gradient accumulator (shared memory or A->grad)
+    V3 dL, Ltot;     // dLoss/dL of the path and its forward radiance
+    int mat;
+    bool mollify;
+    float mollified;
+    V3 beta;         // throughput at the current surface vertex
+    bool has_nee;
+    int light;
+    float G[grad::kParams];  // next-event term's parameter gradient (minus the sampled-f part)
+    V3 gle;                  // next-event term's light-emission gradient
+
+    __device__ __forceinline__ void material(const PathState& ps, float prevRough) {
+        mat = ps.matID;
+        mollify = (P->flags & F_MOLLIFY) && ps.depth > 0;
+        mollified = mixf(0.0f, prevRough, P->mollify_amt);
+    }
+    __device__ __forceinline__ void emitter(const PathState& ps, float misWeight, const HitRecord& hr) {
+        if (hr.light < 0 || hr.light >= A->num_lights) return;
+        float* g = acc + A->num_materials * grad::kParams + 3 * hr.light;
+        atomicAdd(g + 0, dL.x * ps.throughput.x * misWeight);
+        atomicAdd(g + 1, dL.y * ps.throughput.y * misWeight);
+        atomicAdd(g + 2, dL.z * ps.throughput.z * misWeight);
+    }
+    __device__ __forceinline__ void vertex(const PathState& ps) {
+        beta = ps.throughput;
+        has_nee = false;
+    }
+    // out[k] += sum_c w1_c df_c/dtheta_k (and the same with w2 into out2)
+    template <bool TWO>
+    __device__ __forceinline__ void df(float eta, V3 V, V3 N, V3 L, V3 w1, V3 w2, float* out, float* out2) const {
+        constexpr int NC = 4;
+#pragma unroll 1
+        for (int chunk = 0; chunk * NC < grad::kParams; ++chunk) {
+            const grad::MatD<NC> m = grad::LoadMaterialD<NC>(P->mats, mat, chunk, mollify, mollified);
+            const grad::DV3<NC> f = grad::DisneyEvalD(m, eta, V, N, L);
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const int q = chunk * NC + k;
+                if (q < grad::kParams) {
+                    out[q] += w1.x * f.x.d[k] + w1.y * f.y.d[k] + w1.z * f.z.d[k];
+                    if (TWO) out2[q] += w2.x * f.x.d[k] + w2.y * f.y.d[k] + w2.z * f.z.d[k];
+                }
+            }
+        }
+    }
+    __device__ __forceinline__ void nee_light(int index, float misWeight, V3 Li, V3 sf, float lightPdf, float eta,
+                                              V3 V, V3 N, V3 L) {
+        has_nee = true;
+        light = index;
+#pragma unroll
+        for (int k = 0; k < grad::kParams; ++k) G[k] = 0.0f;
+        const float s = misWeight / lightPdf;
+        df<false>(eta, V, N, L, dL * beta * Li * s, v3(0.0f), G, nullptr);
+        gle = dL * beta * sf * (s * (float)P->num_lights);
+    }
+    __device__ __forceinline__ void sample(float eta, V3 V, V3 N, V3 L, V3 f, const PathState& ps,
+                                           const ShadowReq& sr) {
+        const V3 rest = Ltot - ps.radiance;  // the terms after this vertex, plus its next-event term
+        const V3 nee = (has_nee && (sr.adds & 2)) ? sr.contrib[1] * sr.T : v3(0.0f);
+        V3 wu, wn;
+        wu.x = f.x != 0.0f ? dL.x * rest.x / f.x : 0.0f;
+        wu.y = f.y != 0.0f ? dL.y * rest.y / f.y : 0.0f;
+        wu.z = f.z != 0.0f ? dL.z * rest.z / f.z : 0.0f;
+        wn.x = f.x != 0.0f ? dL.x * nee.x / f.x : 0.0f;
+        wn.y = f.y != 0.0f ? dL.y * nee.y / f.y : 0.0f;
+        wn.z = f.z != 0.0f ? dL.z * nee.z / f.z : 0.0f;
+        float U[grad::kParams], W[grad::kParams];
+#pragma unroll
+        for (int k = 0; k < grad::kParams; ++k) U[k] = W[k] = 0.0f;
+        df<true>(eta, V, N, L, wu, wn, U, W);
+        float* g = acc + mat * grad::kParams;
+#pragma unroll
+        for (int k = 0; k < grad::kParams; ++k) {
+            if (U[k] != 0.0f) atomicAdd(g + k, U[k]);
+            G[k] -= W[k];  // applies only with the next-event term (unoccluded)
+        }
+    }
+};
+
+__device__ __forceinline__ float* adj_accumulator(const AdjView& A, float* sgrad) {
+    if (!A.shared) return A.grad;
+    for (int k = threadIdx.x; k < A.grad_size; k += blockDim.x) sgrad[k] = 0.0f;
+    __syncthreads();
+    return sgrad;
+}
+__device__ __forceinline__ void adj_flush(const AdjView& A, const float* sgrad) {
+    if (!A.shared) return;
+    __syncthreads();
+    for (int k = threadIdx.x; k < A.grad_size; k += blockDim.x)
+        if (sgrad[k] != 0.0f) atomicAdd(A.grad + k, sgrad[k]);
+}
+
+template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false>
+__global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
     uint2 stack[INLINE ? kStackSize : 1];
+    extern __shared__ float sgrad[];
+    float* acc = nullptr;
+    if (ADJ) acc = adj_accumulator(A, sgrad);
     const int n = B.counts[in];
     Counters cnt{0, 0};
     for (int j0 = blockIdx.x * blockDim.x; j0 < n; j0 += gridDim.x * blockDim.x) {
@@ -204,10 +320,35 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
             hr.prim = h1.x; hr.inst = h1.y; hr.mat = h1.z;
             hr.hit = h1.w & 1;
             hr.isEmitter = (h1.w >> 1) & 1;
+            hr.light = h1.w >> 2;
             hr.lightEmission = v3(h2.x, h2.y, h2.z);
             hr.lightPdf = h2.w;
             ShadowReq sr;
-            cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt);
+            if constexpr (ADJ) {
+                AdjHook h;
+                h.P = &P;
+                h.A = &A;
+                h.acc = acc;
+                const int npix = W.w * W.h, pix = i % npix;
+                const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+                const float* di = A.dimage + 3 * ((size_t)py * A.width + px);
+                h.dL = v3(di[0], di[1], di[2]) * A.inv_passes;
+                const float4 lt = B.rad[i];
+                h.Ltot = v3(lt.x, lt.y, lt.z);
+                h.has_nee = false;
+                h.light = -1;
+                cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, h);
+                const bool deferred = h.has_nee && (sr.n & 2) && (sr.adds & 2);
+                if (deferred) {
+                    A.v[3 * (size_t)i] = make_float4(h.G[0], h.G[1], h.G[2], h.G[3]);
+                    A.v[3 * (size_t)i + 1] = make_float4(h.G[4], h.G[5], h.G[6], h.G[7]);
+                    A.v[3 * (size_t)i + 2] = make_float4(h.G[8], h.G[9], h.G[10], __int_as_float(h.mat));
+                }
+                A.le[i] = make_float4(h.gle.x, h.gle.y, h.gle.z, __int_as_float(deferred ? h.light : -1));
+            } else {
+                NoHook nh;
+                cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, nh);
+            }
             if (cont && ps.depth > 65536) {  // alpha pass-through loops are bounded (pt_kernels.cu)
                 flag_status(P.status, PT_ERR_TIMEOUT);
                 cont = false;
@@ -234,14 +375,19 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in) {
         push(B.qs, B.counts + 2, i, valid && shadow);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
+    if (ADJ) adj_flush(A, sgrad);
 }
 
 // Any-hit queries of the shadow queue (one or two rays per path: the env
 // sample first, then the light sample), persistent like wf_extend, with the
 // same batched retire / refill.  The deferred form is used only when AnyHit
 // draws no random numbers.
-__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refill, int min_tris) {
+template <bool ADJ = false>
+__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refill, int min_tris, AdjView A) {
     uint2 stack[kStackSize];
+    extern __shared__ float sgrad[];
+    float* acc = nullptr;
+    if (ADJ) acc = adj_accumulator(A, sgrad);
     const int n = B.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
     Counters cnt{0, 0};
@@ -298,6 +444,22 @@ __global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refi
             L.z = rad.z;
             B.L[i] = L;
             if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+            if (ADJ && (sr.adds & 2) && !occ1) {  // the next-event term counts: its gradients too
+                const float4 le = A.le[i];
+                const int light = __float_as_int(le.w);
+                if (light >= 0) {
+                    const float4 v0 = A.v[3 * (size_t)i], v1 = A.v[3 * (size_t)i + 1], v2 = A.v[3 * (size_t)i + 2];
+                    float* g = acc + __float_as_int(v2.w) * grad::kParams;
+                    const float gv[grad::kParams] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w, v2.x, v2.y, v2.z};
+#pragma unroll
+                    for (int k = 0; k < grad::kParams; ++k)
+                        if (gv[k] != 0.0f) atomicAdd(g + k, gv[k]);
+                    float* gl = acc + A.num_materials * grad::kParams + 3 * light;
+                    atomicAdd(gl + 0, le.x);
+                    atomicAdd(gl + 1, le.y);
+                    atomicAdd(gl + 2, le.z);
+                }
+            }
         }
     };
     for (;;) {
@@ -338,6 +500,7 @@ __global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refi
         }
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
+    if (ADJ) adj_flush(A, sgrad);
 }
 
 __global__ void __launch_bounds__(256) wf_resolve(Params P, RenderWork W, WfView B, int npass) {
@@ -371,7 +534,7 @@ WfView view_of(const WavefrontBuffers& wb) {
 
 template <int MEDIUM, bool ENV, bool INLINE>
 cudaError_t launch_shade(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
-    wf_shade<MEDIUM, ENV, INLINE><<<grid, block, 0, s>>>(p, v, in);
+    wf_shade<MEDIUM, ENV, INLINE><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
     return cudaGetLastError();
 }
 
@@ -551,7 +714,7 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
                        [&] { return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
             return e;
         if ((e = timed(timer, STAGE_SHADOW, s, [&] {
-                 wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris);
+                 wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris, AdjView{});
                  return cudaGetLastError();
              })) != cudaSuccess)
             return e;
@@ -622,7 +785,7 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
                 const int in = it & 1;
                 wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
                 if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
-                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris);
+                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris, AdjView{});
                 if ((e = cudaGetLastError()) != cudaSuccess) return e;
                 nl += 3;
             }
@@ -638,6 +801,39 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
     return cudaSuccess;
 }
 
+cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
+                           const AdjView& A, bool run_forward, cudaStream_t s, int* launches) {
+    int dummy = 0;
+    int& nl = launches ? *launches : dummy;
+    nl = 0;
+    if (W.w <= 0 || W.h <= 0 || W.num_passes <= 0) return cudaSuccess;
+    if ((long)W.w * W.h * W.num_passes > wb.capacity) return cudaErrorInvalidValue;
+    const int iterations = p.max_depth + 1;
+    cudaError_t e;
+    if (run_forward) {
+        if ((e = enqueue_batch(p, W, wb, W.first_pass, W.num_passes, iterations, t, s, nullptr)) != cudaSuccess)
+            return e;
+        nl += 1 + 3 * iterations;
+    }
+    const WfView v = view_of(wb);
+    const int n = W.w * W.h * W.num_passes;
+    const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
+    const size_t smem = A.shared ? sizeof(float) * (size_t)A.grad_size : 0;
+    wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, W.first_pass, W.num_passes);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    for (int it = 0; it < iterations; ++it) {
+        const int in = it & 1;
+        wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        wf_shade<0, false, false, true><<<t.shade_grid, t.shade_block, smem, s>>>(p, v, in, W, A);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        wf_shadow<true><<<t.shadow_grid, t.shadow_block, smem, s>>>(p, v, t.shadow_refill, t.min_tris, A);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    nl += 1 + 3 * iterations;
+    return cudaSuccess;
+}
+
 cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -646,7 +842,7 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     int b_ext = 0, b_shade = 0, b_shadow = 0, b256 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_ext, wf_extend, block, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shade, wf_shade<0, false, false>, block, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shadow, wf_shadow, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shadow, wf_shadow<false>, block, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b256, wf_resolve, 256, 0);
     t.extend_block = t.shade_block = t.shadow_block = block;
     t.extend_grid = sms * std::max(1, b_ext);

@@ -31,7 +31,7 @@ struct WavefrontTuning {
     int extend_block = 128, shade_block = 128, shadow_block = 128;
     // idle lanes of a warp that trigger a retire + refill round in the
     // persistent extend / shadow kernels (PT_WAVEFRONT_REFILL overrides)
-    int extend_refill = 8, shadow_refill = 8;
+    int extend_refill = 12, shadow_refill = 12;
     // triangle steps run when at least min_tris lanes of a warp have
     // triangles pending; fewer are postponed (0: every lane steps on its own;
     // PT_WAVEFRONT_MIN_TRIS overrides).  Needs trav_postpone_fits(depth).
@@ -65,6 +65,30 @@ cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb);
 cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity);
 void wavefront_free(WavefrontBuffers& wb);
 cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block);
+// Inputs and outputs of the adjoint (path-replay backpropagation) batch.
+// The loss gradient dLoss/dI is given per pixel of the full frame, with
+// I = accumulation / num_passes; per path, dLoss/dL = dLoss/dI / num_passes.
+// Gradients: 11 per material (pt_grad.cuh's parameter order), then 3 per
+// light (emission r, g, b).
+struct AdjView {
+    const float* dimage = nullptr;  // 3 floats per full-frame pixel
+    float inv_passes = 1.0f;
+    int width = 0;                  // full-frame width (row stride of dimage)
+    float* grad = nullptr;
+    int num_materials = 0, num_lights = 0;
+    int grad_size = 0;              // floats of grad
+    int shared = 0;                 // accumulate per block in shared memory first
+    float4* v = nullptr;            // 3 per path: deferred next-event gradient (11 values + material)
+    float4* le = nullptr;           // 1 per path: light-emission gradient + light index (-1: none)
+};
+
+// The adjoint batch for the work W (one batch: W.num_passes * pixels must
+// fit the buffers).  run_forward: trace the forward batch first (no
+// accumulation) so that each path's radiance is in the buffers; otherwise
+// they must hold the forward batch of the same work already.
+cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
+                           const AdjView& A, bool run_forward, cudaStream_t s, int* launches = nullptr);
+
 // *launches (if given) receives the number of kernels launched; with a
 // timer, every launch is timed (and no graph is used).
 cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,

@@ -154,6 +154,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_render_tile.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.pt_render_tile_noalloc.argtypes = [P, C.c_int32, C.c_int32, C.c_int32]
     lib.pt_render_passes.argtypes = [P, C.c_int32, C.c_int32]
+    lib.pt_update_materials.argtypes = [P, _f, C.c_int32]
+    lib.pt_update_lights.argtypes = [P, _f, C.c_int32]
+    lib.pt_render_adjoint.argtypes = [P, C.c_int32, C.c_int32, _f, _f]
     lib.pt_get_accum.argtypes = [P, _f]
     lib.pt_snapshot_accum.argtypes = [P]
     lib.pt_get_output.argtypes = [P, C.c_int32, C.c_int32, _u8]
@@ -167,6 +170,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in ("pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
+                 "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
                  "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
                  "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing",
                  "pt_get_stage_stats", "pt_get_stats", "pt_last_error"):
@@ -179,6 +183,7 @@ def load_library(path: str | None = None) -> C.CDLL:
 HEADER_SYMBOLS = [
     "pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
     "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_tile_noalloc",
+    "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
     "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
     "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing", "pt_get_stage_stats", "pt_get_stats",
     "pt_last_error",

@@ -99,6 +99,25 @@ class GpuRenderer:
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
                     status=s.status, launches=s.kernel_launches)
 
+    def update_materials(self, materials: np.ndarray):
+        m = np.ascontiguousarray(materials, np.float32)
+        self._ck(self.lib.pt_update_materials(self.ctx, m.ctypes.data_as(C.POINTER(C.c_float)), m.shape[0]))
+
+    def update_lights(self, lights: np.ndarray):
+        m = np.ascontiguousarray(lights, np.float32)
+        self._ck(self.lib.pt_update_lights(self.ctx, m.ctypes.data_as(C.POINTER(C.c_float)), m.shape[0]))
+
+    def render_adjoint(self, first_pass: int, num_passes: int, d_image: np.ndarray) -> np.ndarray:
+        """Gradient of a loss of I = accum / num_passes (d_image = dLoss/dI,
+        H x W x 3) w.r.t. 11 parameters per material, then 3 per light."""
+        di = np.ascontiguousarray(d_image, np.float32)
+        assert di.shape == (self.height, self.width, 3)
+        n = self.scene.materials.shape[0] * 11 + self.scene.lights.shape[0] * 3
+        g = np.zeros(n, np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._ck(self.lib.pt_render_adjoint(self.ctx, first_pass, num_passes, fp(di), fp(g)))
+        return g
+
     def set_stage_timing(self, on: bool):
         self._ck(self.lib.pt_set_stage_timing(self.ctx, 1 if on else 0))
 

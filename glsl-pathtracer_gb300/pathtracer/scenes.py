@@ -401,6 +401,42 @@ def icosphere_scene(freq=229, width=1920, height=1080, max_depth=8, seed=1, tile
     return build_scene(meshes, instances, mats, [light], cam, opts)
 
 
+def diff_scene(freq=229, width=512, height=512, max_depth=6, num_materials=32, seed=1, tile=None) -> SceneData:
+    """The differentiable-materials workload: the displaced icosphere split
+    into num_materials meshes by icosahedron face (face % num_materials), one
+    material each with every Disney lobe active -- baseColor U[0.05,0.95]^3,
+    metallic, roughness, subsurface, specularTint, sheen, sheenTint,
+    clearcoat U[0.05,0.95], clearcoatGloss U[0.05,0.95] -- and four sphere
+    lights of radius 0.5 around the camera side of the sphere."""
+    V, Fc, face = icosphere(freq, 1.0, 0.05, seed)
+    rng = np.random.RandomState(seed + 200)
+    mats = [material()]
+    for k in range(num_materials):
+        u = rng.uniform(0.05, 0.95, 11)
+        mats.append(material(color=tuple(u[0:3]), metallic=float(u[3]), roughness=float(u[4]),
+                             subsurface=float(u[5]), specular_tint=float(u[6]), sheen=float(u[7]),
+                             sheen_tint=float(u[8]), clearcoat=float(u[9]), clearcoat_gloss=float(u[10]), ior=1.5))
+    fn = np.cross(V[Fc[:, 1]] - V[Fc[:, 0]], V[Fc[:, 2]] - V[Fc[:, 0]])
+    Nv = np.zeros_like(V)
+    for k in range(3):
+        np.add.at(Nv, Fc[:, k], fn)
+    Nv /= np.maximum(np.linalg.norm(Nv, axis=1, keepdims=True), 1e-30)
+    meshes, instances = [], []
+    ident = mat4()
+    for g in range(num_materials):
+        sel = Fc[(face % num_materials) == g]
+        meshes.append(mesh_from_indexed(V, sel, Nv))
+        instances.append((g, g + 1, ident))
+    lights = [sphere_light((2.2, 2.4, 2.6), 0.5, (20.0, 18.0, 16.0)),
+              sphere_light((-2.4, 1.8, 2.2), 0.5, (8.0, 10.0, 14.0)),
+              sphere_light((2.0, -2.2, 2.4), 0.5, (12.0, 9.0, 6.0)),
+              sphere_light((-2.0, -2.0, 2.8), 0.5, (6.0, 12.0, 8.0))]
+    cam = camera((0.0, 0.0, 3.2), (0.0, 0.0, 0.0), 45.0)
+    opts = dict(render_width=width, render_height=height, tile_width=tile or 256, tile_height=tile or 256,
+                max_depth=max_depth)
+    return build_scene(meshes, instances, mats, lights, cam, opts)
+
+
 def sky_envmap(width=2048, height=1024, sun_dir=(0.4, 0.7, 0.3), sun_radius_deg=0.5, sun_intensity=5.0e4):
     """Synthetic equirect HDR in the reference's mapping (envmap.glsl:57-66):
     sky gradient 0.5 (horizon and below) to 1.5 (zenith) plus a sun disc."""

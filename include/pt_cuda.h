@@ -210,6 +210,36 @@ int pt_render_tile(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t fram
  * pt_render_tile adds to (clear it with pt_clear_accum). */
 int pt_render_tile_noalloc(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t frame_num);
 
+/* Replaces: the material re-upload of Renderer::Update's instancesModified
+ * branch (src/core/Renderer.cpp:654-656) on its own: new values for the
+ * num_materials materials (the count cannot change). */
+int pt_update_materials(pt_context* ctx, const float* materials, int32_t num_materials);
+
+/* No counterpart in the reference (its lights are uploaded once, at
+ * Renderer::InitGPUDataBuffers): new light values, 15 floats each
+ * (GLSLPT::Light); the count cannot change. */
+int pt_update_lights(pt_context* ctx, const float* lights, int32_t num_lights);
+
+/* Differentiable rendering (no counterpart in the reference): gradient of a
+ * loss of the image I = accumulation / num_passes of sample passes
+ * first_pass .. first_pass+num_passes-1 (the work of pt_render_passes) with
+ * respect to the material parameters and light emissions, by path-replay
+ * backpropagation with the wavefront integrator.
+ *   d_image  dLoss/dI, 3 floats (r, g, b) per pixel, rows from the bottom
+ *   grad     out: 11 floats per material -- baseColor r, g, b, metallic,
+ *            roughness, subsurface, specularTint, sheen, sheenTint,
+ *            clearcoat, clearcoatGloss (the raw GLSLPT::Material values) --
+ *            then 3 per light (emission r, g, b)
+ * Sampling is detached (directions, lobe and light choices, MIS weights and
+ * Russian roulette are held fixed), so the result is the gradient of the
+ * expected image.  When the last pt_render_passes call was the same work
+ * with the wavefront integrator and nothing changed since, its per-path
+ * radiance is reused; otherwise the forward paths are traced first (without
+ * adding to the accumulation).  Media, alpha-tested materials and
+ * environment maps are not supported (PT_ERR_UNSUPPORTED). */
+int pt_render_adjoint(pt_context* ctx, int32_t first_pass, int32_t num_passes, const float* d_image,
+                      float* grad);
+
 /* Whole-frame form of the same work: sample passes first_pass ..
  * first_pass+num_passes-1, each pass being every tile in the reference's
  * order (Renderer.cpp:745-762), with the frame numbers the tile state machine

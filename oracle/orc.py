@@ -40,6 +40,7 @@ def lib():
         _lib.orc_bsdf_sample.argtypes = [C.c_int, P, P, P, P, C.c_int, P, P, P]
         _lib.orc_camera_rays.argtypes = [P, P, C.c_int, C.c_int, P, P, P, P]
         _lib.orc_rng_stream.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, P]
+        _lib.orc_render_detached.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P]
     return _lib
 
 
@@ -61,6 +62,19 @@ def render(scene, options, camera, first_pass=0, num_passes=1, use_double=False,
     assert rc == 0
     keys = ["closest", "shadow", "nodes", "tris", "overflow", "paths", "tri_hits", "nodes_any", "tris_any"]
     return accum, sq, dict(zip(keys, [int(x) for x in cnt]))
+
+
+def render_detached(scene, eval_scene, options, camera, first_pass=0, num_passes=1, use_double=True, nthreads=0):
+    """The detached estimator: sampling from `scene`, BSDF and emission values
+    from `eval_scene` (same geometry).  Returns the mean radiance per pixel,
+    H x W x 3 float64 (sum over the passes / num_passes)."""
+    W, H = options.render_width, options.render_height
+    acc = np.zeros((H, W, 3), np.float64)
+    d, e = scene.desc(), eval_scene.desc()
+    rc = lib().orc_render_detached(C.byref(d), C.byref(e), C.byref(options), C.byref(camera), first_pass,
+                                   num_passes, int(use_double), nthreads, _p(acc))
+    assert rc == 0
+    return acc / num_passes
 
 
 def closest_hit_full(scene, rays):

@@ -199,6 +199,44 @@ int orc_trace_any(const pt_scene_desc* d, const pt_render_options* o, const pt_r
     return use_double ? trace_any_impl<double>(d, o, rays, maxd, n, occ) : trace_any_impl<float>(d, o, rays, maxd, n, occ);
 }
 
+// The detached estimator (PathTraceDetached) of sample passes
+// [first_pass, first_pass+num_passes): sampling from scene d, values from
+// scene e (same geometry, other materials / lights).  ADDS radiance (RGB,
+// FP64 sums) into accum (W*H*3 doubles).
+int orc_render_detached(const pt_scene_desc* d, const pt_scene_desc* e, const pt_render_options* o,
+                        const pt_camera* cam, int first_pass, int num_passes, int use_double, int nthreads,
+                        double* accum) {
+    auto run = [&](auto tag) {
+        using R = decltype(tag);
+        Scene<R> s, se;
+        MakeScene(s, d, o);
+        MakeScene(se, e, o);
+        const int W = o->render_width, H = o->render_height;
+        if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int py = 0; py < H; ++py) {
+            Counters cnt;
+            for (int px = 0; px < W; ++px) {
+                double* a = accum + 3 * ((size_t)py * W + px);
+                for (int pass = first_pass; pass < first_pass + num_passes; ++pass) {
+                    const int tx = px / o->tile_width, ty = py / o->tile_height;
+                    const int lx = px - tx * o->tile_width, ly = py - ty * o->tile_height;
+                    Rng rng;
+                    rng.init((uint32_t)lx, (uint32_t)ly, FrameNumber(*o, pass, tx, ty));
+                    Ray<R> ray = CameraRay<R>(*cam, *o, px, py, rng);
+                    V3<R> L = PathTraceDetached(s, se, ray, rng, cnt);
+                    a[0] += double(L.x);
+                    a[1] += double(L.y);
+                    a[2] += double(L.z);
+                }
+            }
+        }
+    };
+    if (use_double) run(double{});
+    else run(float{});
+    return 0;
+}
+
 int orc_bsdf_eval(int n, const float* state_params, const float* V, const float* N, const float* L, int use_double,
                   double* f, double* pdf, double* lobe_f, double* lobe_pdf) {
     return use_double ? bsdf_eval_impl<double>(n, state_params, V, N, L, f, pdf, lobe_f, lobe_pdf)

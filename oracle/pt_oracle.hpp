@@ -1326,6 +1326,96 @@ template <class R> inline V3<R> PathTrace(const Scene<R>& s, Ray<R> r, Rng& rng,
     return radiance;
 }
 
+// ------------------------------------------------------ detached estimator
+// PathTrace with the sampling held at one parameter set and the values taken
+// at another: directions, lobe and light choices, MIS weights and Russian
+// roulette come from scene `s` (parameters theta0) exactly as PathTrace
+// draws them, while BSDF values, material emission and light emission come
+// from `e` (the same scene with parameters theta).  Its expectation is the
+// image at theta; at theta = theta0 it is PathTrace itself.  Its derivative
+// in theta is what path-replay backpropagation estimates, so finite
+// differences of it (in R = double) check the adjoint pass.  Surfaces and
+// analytic lights only: no media, alpha test, environment map or roughness
+// mollification.
+template <class R> inline V3<R> PathTraceDetached(const Scene<R>& s, const Scene<R>& e, Ray<R> r, Rng& rng,
+                                                  Counters& cnt) {
+    V3<R> radiance(R(0));
+    V3<R> throughput(R(1));    // at theta (values)
+    V3<R> throughput0(R(1));   // at theta0 (Russian roulette)
+    State<R> state, stateE;
+    LightSampleRec<R> lightSample;
+    R scatterPdf = 0;
+    const Flags& f = s.f;
+    for (state.depth = 0;; state.depth++) {
+        // same geometry in both scenes: the hit is the same, the light
+        // emission of an emitter hit is theta's
+        bool hit = ClosestHit(e, r, state, lightSample, cnt);
+        if (!hit) {
+            if (!(f.hide_emitters && !(state.depth > 0)) && f.uniform_light)
+                radiance = radiance + e.uniform_light_col * throughput;
+            break;
+        }
+        stateE = state;
+        GetMaterial(s, state, r);
+        GetMaterial(e, stateE, r);
+        radiance = radiance + stateE.mat.emission * throughput;
+        if (f.lights && state.isEmitter) {
+            R misWeight = R(1);
+            if (state.depth > 0) misWeight = PowerHeuristic(scatterPdf, lightSample.pdf);
+            radiance = radiance + misWeight * lightSample.emission * throughput;
+            break;
+        }
+        if (state.depth == f.max_depth) break;
+        // next-event estimation (DirectLight's analytic-light part)
+        if (f.lights) {
+            V3<R> scatterPos = state.fhp + state.normal * K<R>::EPS;
+            LightSampleRec<R> ls;
+            int index = int(R(rng.next()) * R(s.num_lights));
+            Light<R> light{}, lightE{};
+            if (index < s.num_lights) {
+                light = FetchLight(s, index);
+                lightE = FetchLight(e, index);
+            } else {
+                light.radius = light.area = light.type = R(0);
+                lightE = light;
+            }
+            SampleOneLight(s, light, scatterPos, ls, rng);
+            const V3<R> LiE = lightE.emission * R(s.num_lights);
+            if (dot(ls.direction, ls.normal) < R(0)) {
+                Ray<R> shadowRay{scatterPos, ls.direction};
+                bool inShadow = AnyHit(s, shadowRay, ls.dist - K<R>::EPS, rng, cnt);
+                if (!inShadow) {
+                    R sfPdf;
+                    DisneyEval(state, -r.direction, state.ffnormal, ls.direction, sfPdf);
+                    R pdfE;
+                    const V3<R> sfE = DisneyEval(stateE, -r.direction, state.ffnormal, ls.direction, pdfE);
+                    R misWeight = R(1);
+                    if (light.area > R(0)) misWeight = PowerHeuristic(ls.pdf, sfPdf);
+                    if (sfPdf > R(0)) radiance = radiance + misWeight * LiE * sfE / ls.pdf * throughput;
+                }
+            }
+        }
+        V3<R> L;
+        R pdf;
+        const V3<R> f0 = DisneySample(state, -r.direction, state.ffnormal, L, pdf, rng);
+        if (!(pdf > R(0))) break;
+        R pdfE;
+        const V3<R> fE = DisneyEval(stateE, -r.direction, state.ffnormal, L, pdfE);
+        throughput = throughput * (fE / pdf);
+        throughput0 = throughput0 * (f0 / pdf);
+        scatterPdf = pdf;
+        r.direction = L;
+        r.origin = state.fhp + r.direction * K<R>::EPS;
+        if (f.rr && state.depth >= f.rr_depth) {
+            R q = fminR(fmaxR(throughput0.x, fmaxR(throughput0.y, throughput0.z)) + R(0.001), R(0.95));
+            if (R(rng.next()) > q) break;
+            throughput = throughput / q;
+            throughput0 = throughput0 / q;
+        }
+    }
+    return radiance;
+}
+
 // ------------------------------------------------------------ camera ray
 // tile.glsl:41-74 for pixel (px, py) of the full frame.  The reference
 // renders tile (tx, ty) of tileW x tileH into a viewport at the origin, so
