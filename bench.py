@@ -13,6 +13,10 @@ segments), counted on the device.
   e2e        through the public C ABI with host buffers, wall clock per step:
              pt_set_camera + pt_render_passes + pt_get_output (tonemapped
              RGBA8 image copied to pinned host memory).
+  adjoint    the differentiable-materials workload (1M-triangle icosphere
+             in 32 materials + 4 lights, 512x512, 16 spp, depth 6): device
+             time of pt_render_adjoint (gradient of 375 parameters, reusing
+             the forward paths) over that of the forward render.
   compare    the megakernel on the same frame and timing rules (it gives the
              same accumulation bit for bit, so equal RMSE): the
              wavefront / megakernel ratio.
@@ -50,7 +54,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import numpy as np  # noqa: E402
 
-METRIC = "Mrays/s @1080p depth8 1M tris"
+METRIC = "Mrays/s @1080p depth8 1M tris: wavefront vs megakernel, equal RMSE; adjoint/fwd"
 CONFIGS = {
     "icosphere_1m": dict(desc="icosphere 1,048,820 tris, 1920x1080, 16 spp, depth 8", freq=229, width=1920,
                          height=1080, spp=16, depth=8),
@@ -216,6 +220,43 @@ def run_reference(args, cfg, name):
     print(json.dumps(line))
 
 
+ADJOINT_WORKLOAD = ("differentiable materials: icosphere 1,048,820 tris split into 32 materials (11 Disney "
+                    "parameters each) + 4 sphere lights (emission rgb), 512x512, 16 spp, depth 6")
+
+
+def adjoint_bench(steps, stream, flush):
+    """Forward and adjoint (pt_render_adjoint, reusing the forward paths) of
+    the differentiable-materials workload; device time of each call from the
+    library's own CUDA events."""
+    import torch
+    from pathtracer import capi, diff, scenes
+    from pathtracer.renderer import GpuRenderer
+    sd = scenes.diff_scene(freq=229, width=512, height=512, max_depth=6)
+    dI = np.random.RandomState(4).normal(size=(512, 512, 3)).astype(np.float32)
+    fwd, adj = [], []
+    with GpuRenderer(sd) as r:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        r.set_stream(stream.cuda_stream)
+        for k in range(steps + 1):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+            r.render_passes(16 * k, 16)
+            st = r.stats()
+            g = r.render_adjoint(16 * k, 16, dI)
+            sa = r.stats()
+            if k > 0:  # the first round is warm-up
+                fwd.append((st["kernel_ms"], st["closest"] + st["shadow"]))
+                adj.append(sa["kernel_ms"])
+        r.set_stream(None)
+    f_ms = statistics.mean(m for m, _ in fwd)
+    a_ms = statistics.mean(adj)
+    rays = statistics.mean(n for _, n in fwd)
+    return {"workload": ADJOINT_WORKLOAD, "params": diff.num_params(sd.materials, sd.lights),
+            "forward_ms": f_ms, "adjoint_ms": a_ms, "adjoint_over_forward": a_ms / f_ms,
+            "forward_mrays_s": rays / (f_ms / 1000.0) / 1e6, "steps": steps,
+            "grad_finite": bool(np.isfinite(g).all())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,6 +268,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=3,
                     help="timed steps of the other integrator, for the wavefront/megakernel ratio (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=3,
+                    help="steps of the differentiable-materials workload for adjoint/forward (0: skip)")
     ap.add_argument("--stage-steps", type=int, default=3,
                     help="extra steps timed per kernel with CUDA events (roofline of the dominant kernel)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
@@ -351,6 +394,10 @@ def main():
         stages = {"ms": {k: v[0] for k, v in tot.items()}, "launches": {k: v[1] for k, v in tot.items()},
                   "rays": st_rays, "steps": args.stage_steps}
 
+    adjoint = None
+    if args.adjoint_steps > 0 and rank == 0 and not args.small:
+        adjoint = adjoint_bench(args.adjoint_steps, stream, flush)
+
     # end to end through the C ABI with host buffers
     import ctypes as C
     lib = capi.load_library()
@@ -420,6 +467,8 @@ def main():
         }
         if other:
             line["compare"] = other
+        if adjoint:
+            line["adjoint"] = adjoint
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
