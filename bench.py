@@ -237,6 +237,7 @@ def adjoint_bench(steps, stream, flush):
     with GpuRenderer(sd) as r:
         r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
         r.set_stream(stream.cuda_stream)
+        r.autotune(2)
         for k in range(steps + 1):
             with torch.cuda.stream(stream):
                 flush.fill_(k & 0xFF)
@@ -268,6 +269,7 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=3,
                     help="timed steps of the other integrator, for the wavefront/megakernel ratio (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
     ap.add_argument("--adjoint-steps", type=int, default=3,
                     help="steps of the differentiable-materials workload for adjoint/forward (0: skip)")
     ap.add_argument("--stage-steps", type=int, default=3,
@@ -302,6 +304,9 @@ def main():
     stream = torch.cuda.Stream()
     r.set_stream(stream.cuda_stream)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    tuning = None
+    if args.integrator == "wavefront" and not args.no_autotune:
+        tuning = r.autotune(2)  # set-up, before the timed region
     # each rank renders its own range of sample passes of the same frame
     pass_base = rank * spp * (args.steps + args.warmup + 8)
 
@@ -459,7 +464,8 @@ def main():
             "config": {"workload": cfg["desc"] + ("" if not args.small else " (small variant)"),
                        "integrator": args.integrator, "rays_per_step": rays_per_step,
                        "l2": "flushed before each timed step (512 MiB write)",
-                       "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU"},
+                       "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU",
+                       "tuning": tuning if tuning else "default"},
             "gpu_launches": launches,
             "roofline": roofline,
             "e2e": e2e,

@@ -798,6 +798,144 @@ int pt_bsdf_sample(pt_context* c, const float* rec, const float* V, const float*
     return PT_OK;
 }
 
+namespace {
+void tuning_out(const WavefrontTuning& t, float ms, pt_tuning* out) {
+    out->extend_variant = t.extend_variant;
+    out->shadow_variant = t.shadow_variant;
+    out->extend_refill = t.extend_refill;
+    out->shadow_refill = t.shadow_refill;
+    out->min_tris = t.min_tris;
+    out->frame_ms = ms;
+}
+}  // namespace
+
+int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
+    if (!c || !out || num_passes <= 0) return set_err(PT_ERR_INVALID_ARG, "invalid argument");
+    RenderWork w;
+    w.x0 = w.y0 = 0;
+    w.w = c->opts.render_width;
+    w.h = c->opts.render_height;
+    w.first_pass = 0;
+    w.num_passes = num_passes;
+    w.tile_frame = -1;
+    w.tile_x = w.tile_y = 0;
+    const int cap = wavefront_capacity(c, w);
+    if (c->wf.capacity < cap) CK(wavefront_alloc(c->wf, cap));
+    if (!c->wf_tuned) {
+        CK(wavefront_default_tuning(c->wf_tuning, 128));
+        c->wf_tuned = true;
+    }
+    // the candidates render into a scratch accumulation; the caller's is kept
+    DevBuf<float4> scratch;
+    CK(scratch.alloc(c->accum.n));
+    std::swap(c->accum, scratch);
+    const bool postpone = trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth);
+    StageTimer timer;
+    int rc = PT_OK;
+    // device time per stage of a frame with tuning t: the faster of two
+    // timed frames after one untimed one
+    auto measure = [&](const WavefrontTuning& t, float ms[STAGE_COUNT]) -> int {
+        for (int k = 0; k < STAGE_COUNT; ++k) ms[k] = 1e30f;
+        Params p = make_params(c);
+        for (int rep = 0; rep < 3; ++rep) {
+            timer.reset();
+            CK(launch_wavefront(p, w, c->wf, t, false, c->stream, nullptr, rep ? &timer : nullptr));
+            if (!rep) continue;
+            float m[STAGE_COUNT];
+            int n[STAGE_COUNT];
+            CK(timer.summarise(m, n));
+            for (int k = 0; k < STAGE_COUNT; ++k) ms[k] = std::min(ms[k], m[k]);
+        }
+        return PT_OK;
+    };
+    WavefrontTuning best = c->wf_tuning;
+    if (!postpone) best.min_tris = 0;
+    float ms[STAGE_COUNT];
+    do {
+        // 1. kernel variants, extend and shadow chosen separately
+        float be = 1e30f, bs = 1e30f;
+        int ve = best.extend_variant, vs = best.shadow_variant;
+        for (int v = 0; v < 4; ++v) {
+            WavefrontTuning t = best;
+            t.extend_variant = t.shadow_variant = v;
+            if ((rc = measure(t, ms))) break;
+            if (ms[STAGE_EXTEND] < be) { be = ms[STAGE_EXTEND]; ve = v; }
+            if (ms[STAGE_SHADOW] < bs) { bs = ms[STAGE_SHADOW]; vs = v; }
+        }
+        if (rc) break;
+        best.extend_variant = ve;
+        best.shadow_variant = vs;
+        // 2. refill thresholds, separately
+        const int refills[] = {4, 8, 12, 16};
+        be = bs = 1e30f;
+        int re = best.extend_refill, rs = best.shadow_refill;
+        for (int r : refills) {
+            WavefrontTuning t = best;
+            t.extend_refill = t.shadow_refill = r;
+            if ((rc = measure(t, ms))) break;
+            if (ms[STAGE_EXTEND] < be) { be = ms[STAGE_EXTEND]; re = r; }
+            if (ms[STAGE_SHADOW] < bs) { bs = ms[STAGE_SHADOW]; rs = r; }
+        }
+        if (rc) break;
+        best.extend_refill = re;
+        best.shadow_refill = rs;
+        // 3. triangle postponement (shared by both stages)
+        if (postpone) {
+            const int mins[] = {0, 4, 8, 12};
+            float bt = 1e30f;
+            int mt = best.min_tris;
+            for (int m : mins) {
+                WavefrontTuning t = best;
+                t.min_tris = m;
+                if ((rc = measure(t, ms))) break;
+                const float tot = ms[STAGE_EXTEND] + ms[STAGE_SHADOW];
+                if (tot < bt) { bt = tot; mt = m; }
+            }
+            if (rc) break;
+            best.min_tris = mt;
+        }
+        if ((rc = measure(best, ms))) break;
+    } while (false);
+    timer.release();
+    std::swap(c->accum, scratch);
+    scratch.free();
+    c->fwd.valid = false;
+    if (rc) return rc;
+    c->wf_tuning = best;
+    float total = 0.0f;
+    for (int k = 0; k < STAGE_COUNT; ++k) total += ms[k];
+    tuning_out(best, total, out);
+    return PT_OK;
+}
+
+int pt_get_tuning(pt_context* c, pt_tuning* out) {
+    if (!c || !out) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (!c->wf_tuned) {
+        CK(wavefront_default_tuning(c->wf_tuning, 128));
+        c->wf_tuned = true;
+    }
+    tuning_out(c->wf_tuning, 0.0f, out);
+    return PT_OK;
+}
+
+int pt_set_tuning(pt_context* c, const pt_tuning* in) {
+    if (!c || !in) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (in->extend_variant < 0 || in->extend_variant > 3 || in->shadow_variant < 0 || in->shadow_variant > 3 ||
+        in->extend_refill < 1 || in->extend_refill > 32 || in->shadow_refill < 1 || in->shadow_refill > 32 ||
+        in->min_tris < 0 || in->min_tris > 32)
+        return set_err(PT_ERR_INVALID_ARG, "tuning value out of range");
+    if (!c->wf_tuned) {
+        CK(wavefront_default_tuning(c->wf_tuning, 128));
+        c->wf_tuned = true;
+    }
+    c->wf_tuning.extend_variant = in->extend_variant;
+    c->wf_tuning.shadow_variant = in->shadow_variant;
+    c->wf_tuning.extend_refill = in->extend_refill;
+    c->wf_tuning.shadow_refill = in->shadow_refill;
+    c->wf_tuning.min_tris = in->min_tris;
+    return PT_OK;
+}
+
 int pt_set_stage_timing(pt_context* c, int32_t on) {
     if (!c) return set_err(PT_ERR_INVALID_ARG, "context is NULL");
     c->stage_timing = on != 0;

@@ -66,6 +66,32 @@ __device__ __forceinline__ float qbyte_biased(uint32_t w, int j) {
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j));
 }
 
+// Packed FP32 pairs (sm_100+): one instruction for two IEEE round-to-nearest
+// operations, with the results of the two scalar ones.
+__device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
+    unsigned long long r;
+#ifdef __CUDA_ARCH__
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+#else
+    r = (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
+#endif
+    return r;
+}
+// ((a - b) * c + d) per lane of the pairs, rounded as fmaf(a - b, c, d)
+__device__ __forceinline__ void f2_sub_fma(unsigned long long a, unsigned long long b, unsigned long long c,
+                                           unsigned long long d, float& lo, float& hi) {
+#ifdef __CUDA_ARCH__
+    unsigned long long t, r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(a), "l"(b));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(t), "l"(c), "l"(d));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+#else
+    auto f = [](unsigned long long v, int k) { return __uint_as_float((uint32_t)(v >> (32 * k))); };
+    lo = fmaf(f(a, 0) - f(b, 0), f(c, 0), f(d, 0));
+    hi = fmaf(f(a, 1) - f(b, 1), f(c, 1), f(d, 1));
+#endif
+}
+
 __device__ __forceinline__ float fmax3f(float a, float b, float c) {
 #ifdef __CUDA_ARCH__
     float d;
@@ -87,7 +113,10 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
 
 // Slab test of the eight children of wide node `idx`; returns the hit mask.
 // Plane distances are (q - 2^23 bias) * (scale / d) + (origin - o) / d; the
-// entry and exit distances are three-input max / min (sm_100+).
+// entry and exit distances are three-input max / min (sm_100+).  PACKED
+// computes the near and far planes of an axis as one packed pair (the same
+// values, fewer instructions, more registers).
+template <bool PACKED = false>
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
                                                    float tmax, uint32_t& child_base, uint32_t& prim_base,
                                                    uint32_t& imask) {
@@ -120,12 +149,23 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
         const uint32_t nzw = nz ? qhiz : qloz, fzw = nz ? qloz : qhiz;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float tnx = fmaf(qbyte_biased(nxw, j) - 8388608.0f, adjx, orgx);
-            const float tfx = fmaf(qbyte_biased(fxw, j) - 8388608.0f, adjx, orgx);
-            const float tny = fmaf(qbyte_biased(nyw, j) - 8388608.0f, adjy, orgy);
-            const float tfy = fmaf(qbyte_biased(fyw, j) - 8388608.0f, adjy, orgy);
-            const float tnz = fmaf(qbyte_biased(nzw, j) - 8388608.0f, adjz, orgz);
-            const float tfz = fmaf(qbyte_biased(fzw, j) - 8388608.0f, adjz, orgz);
+            float tnx, tfx, tny, tfy, tnz, tfz;
+            if (PACKED) {
+                const unsigned long long bias = f2pack(8388608.0f, 8388608.0f);
+                f2_sub_fma(f2pack(qbyte_biased(nxw, j), qbyte_biased(fxw, j)), bias, f2pack(adjx, adjx),
+                           f2pack(orgx, orgx), tnx, tfx);
+                f2_sub_fma(f2pack(qbyte_biased(nyw, j), qbyte_biased(fyw, j)), bias, f2pack(adjy, adjy),
+                           f2pack(orgy, orgy), tny, tfy);
+                f2_sub_fma(f2pack(qbyte_biased(nzw, j), qbyte_biased(fzw, j)), bias, f2pack(adjz, adjz),
+                           f2pack(orgz, orgz), tnz, tfz);
+            } else {
+                tnx = fmaf(qbyte_biased(nxw, j) - 8388608.0f, adjx, orgx);
+                tfx = fmaf(qbyte_biased(fxw, j) - 8388608.0f, adjx, orgx);
+                tny = fmaf(qbyte_biased(nyw, j) - 8388608.0f, adjy, orgy);
+                tfy = fmaf(qbyte_biased(fyw, j) - 8388608.0f, adjy, orgy);
+                tnz = fmaf(qbyte_biased(nzw, j) - 8388608.0f, adjz, orgz);
+                tfz = fmaf(qbyte_biased(fzw, j) - 8388608.0f, adjz, orgz);
+            }
             const float t0 = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
             const float t1 = fmin3f(tfx, tfy, fminf(tfz, tmax));
             if (t0 <= t1) {
@@ -270,7 +310,7 @@ __device__ __forceinline__ bool trav_can_descend(const Trav& s) {
 // Closest hits: the nearest triangle wins; of triangles at exactly the same
 // distance, the one of smallest (triangle, instance) id, so the result does
 // not depend on the order in which triangles are tested.
-template <bool ANY, bool ALPHA>
+template <bool ANY, bool ALPHA, bool PACKED = false>
 __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng, int mode = TRAV_LANE) {
     const bool in_blas = s.cur_inst >= 0;
     if (mode == TRAV_TRIS && !(s.pbits && in_blas)) return TRAV_RUNNING;
@@ -354,7 +394,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         if (s.ng.y > 0x00ffffffu) trav_push(P, stack, s.sp, s.ng);
     }
     uint32_t cb, pb, im;
-    const uint32_t hm = intersect_node(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
+    const uint32_t hm = intersect_node<PACKED>(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
     s.next = -1;
     s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
     s.pbase = pb;

@@ -139,7 +139,8 @@ __device__ __forceinline__ int refill_target(bool exhausted, int refill) { retur
 // unequal the rays are.
 // Traversal is memory-latency bound: 8 blocks of 128 threads (64 registers)
 // keep 32 warps per SM in flight.
-__global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
+template <int MINB, bool PACKED>
+__global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -179,7 +180,8 @@ __global__ void __launch_bounds__(128, 8) wf_extend(Params P, WfView B, int in, 
         const int target = refill_target(exhausted, refill);
         do {
             const int mode = min_tris > 0 ? trav_warp_mode(s, tracing, min_tris) : TRAV_LANE;
-            if (tracing && trav_step<false, false>(s, P, stack, nullptr, mode) != TRAV_RUNNING) tracing = false;
+            if (tracing && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING)
+                tracing = false;
         } while (__popc(__ballot_sync(0xffffffffu, !tracing)) < target);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
@@ -382,8 +384,8 @@ __global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in, Rend
 // sample first, then the light sample), persistent like wf_extend, with the
 // same batched retire / refill.  The deferred form is used only when AnyHit
 // draws no random numbers.
-template <bool ADJ = false>
-__global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refill, int min_tris, AdjView A) {
+template <bool ADJ, int MINB, bool PACKED>
+__global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int refill, int min_tris, AdjView A) {
     uint2 stack[kStackSize];
     extern __shared__ float sgrad[];
     float* acc = nullptr;
@@ -489,7 +491,7 @@ __global__ void __launch_bounds__(128, 8) wf_shadow(Params P, WfView B, int refi
         while (__popc(__ballot_sync(0xffffffffu, !busy)) < target) {
             const int mode = min_tris > 0 ? trav_warp_mode(s, busy, min_tris) : TRAV_LANE;
             if (busy) {
-                const int st = trav_step<true, false>(s, P, stack, nullptr, mode);
+                const int st = trav_step<true, false, PACKED>(s, P, stack, nullptr, mode);
                 if (st != TRAV_RUNNING) {
                     if (stage == 1) occ0 = st == TRAV_HIT;
                     else occ1 = st == TRAV_HIT;
@@ -647,6 +649,38 @@ cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb) {
     return cudaSuccess;
 }
 
+// The traversal kernels come in variants: minimum resident blocks per SM
+// (register budget 64 or 80 per thread) x scalar or packed node test.
+template <int MINB, bool PACKED> static const void* extend_fn() { return (const void*)wf_extend<MINB, PACKED>; }
+template <bool ADJ, int MINB, bool PACKED> static const void* shadow_fn() {
+    return (const void*)wf_shadow<ADJ, MINB, PACKED>;
+}
+
+static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
+    const int g = t.extend_grid_v[t.extend_variant];
+    switch (t.extend_variant) {
+        case 1: wf_extend<8, true><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
+        case 2: wf_extend<6, false><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
+        case 3: wf_extend<6, true><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
+        default: wf_extend<8, false><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
+    }
+    return cudaGetLastError();
+}
+
+template <bool ADJ>
+static cudaError_t launch_shadow(const Params& p, const WfView& v, const WavefrontTuning& t, const AdjView& A,
+                                 size_t smem, cudaStream_t s) {
+    const int g = t.shadow_grid_v[t.shadow_variant];
+    const int b = t.shadow_block, r = t.shadow_refill, m = t.min_tris;
+    switch (t.shadow_variant) {
+        case 1: wf_shadow<ADJ, 8, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        case 2: wf_shadow<ADJ, 6, false><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        case 3: wf_shadow<ADJ, 6, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        default: wf_shadow<ADJ, 8, false><<<g, b, smem, s>>>(p, v, r, m, A); break;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t StageTimer::mark(cudaStream_t s) {
     if (used >= pool.size()) {
         cudaEvent_t e;
@@ -705,18 +739,13 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
     if (e != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
         const int in = it & 1;
-        if ((e = timed(timer, STAGE_EXTEND, s, [&] {
-                 wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
-                 return cudaGetLastError();
-             })) != cudaSuccess)
+        if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, in, t, s); })) != cudaSuccess)
             return e;
         if ((e = timed(timer, STAGE_SHADE, s,
                        [&] { return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
             return e;
-        if ((e = timed(timer, STAGE_SHADOW, s, [&] {
-                 wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris, AdjView{});
-                 return cudaGetLastError();
-             })) != cudaSuccess)
+        if ((e = timed(timer, STAGE_SHADOW, s,
+                       [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s); })) != cudaSuccess)
             return e;
     }
     return cudaSuccess;
@@ -783,10 +812,9 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
                 if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
                 if (count == 0) break;
                 const int in = it & 1;
-                wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
+                if ((e = launch_extend(p, v, in, t, s)) != cudaSuccess) return e;
                 if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
-                wf_shadow<<<t.shadow_grid, t.shadow_block, 0, s>>>(p, v, t.shadow_refill, t.min_tris, AdjView{});
-                if ((e = cudaGetLastError()) != cudaSuccess) return e;
+                if ((e = launch_shadow<false>(p, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
                 nl += 3;
             }
         }
@@ -823,12 +851,10 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
         const int in = it & 1;
-        wf_extend<<<t.extend_grid, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = launch_extend(p, v, in, t, s)) != cudaSuccess) return e;
         wf_shade<0, false, false, true><<<t.shade_grid, t.shade_block, smem, s>>>(p, v, in, W, A);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        wf_shadow<true><<<t.shadow_grid, t.shadow_block, smem, s>>>(p, v, t.shadow_refill, t.min_tris, A);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = launch_shadow<true>(p, v, t, A, smem, s)) != cudaSuccess) return e;
     }
     nl += 1 + 3 * iterations;
     return cudaSuccess;
@@ -840,9 +866,19 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     if (e != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     int b_ext = 0, b_shade = 0, b_shadow = 0, b256 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_ext, wf_extend, block, 0);
+    const void* ext[4] = {extend_fn<8, false>(), extend_fn<8, true>(), extend_fn<6, false>(), extend_fn<6, true>()};
+    const void* shd[4] = {shadow_fn<false, 8, false>(), shadow_fn<false, 8, true>(), shadow_fn<false, 6, false>(),
+                          shadow_fn<false, 6, true>()};
+    for (int k = 0; k < 4; ++k) {
+        int be = 0, bs = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, ext[k], block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, shd[k], block, 0);
+        t.extend_grid_v[k] = sms * std::max(1, be);
+        t.shadow_grid_v[k] = sms * std::max(1, bs);
+    }
+    b_ext = t.extend_grid_v[0] / sms;
+    b_shadow = t.shadow_grid_v[0] / sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shade, wf_shade<0, false, false>, block, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shadow, wf_shadow<false>, block, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b256, wf_resolve, 256, 0);
     t.extend_block = t.shade_block = t.shadow_block = block;
     t.extend_grid = sms * std::max(1, b_ext);
@@ -856,6 +892,10 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     if (const char* r = std::getenv("PT_WAVEFRONT_MIN_TRIS")) {
         const int v = std::atoi(r);
         if (v >= 0 && v <= 32) t.min_tris = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_VARIANT")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v < 4) t.extend_variant = t.shadow_variant = v;
     }
     return cudaSuccess;
 }

@@ -37,6 +37,12 @@ struct WavefrontTuning {
     // PT_WAVEFRONT_MIN_TRIS overrides).  Needs trav_postpone_fits(depth).
     int min_tris = 8;
     int extend_grid = 0, shade_grid = 0, shadow_grid = 0;
+    // kernel variants of the traversal stages: 0 = 8 blocks (64 registers),
+    // scalar node test; 1 = 8 blocks, packed; 2 = 6 blocks (80 registers),
+    // scalar; 3 = 6 blocks, packed (PT_WAVEFRONT_VARIANT overrides); the
+    // persistent grid of each variant fills the GPU
+    int extend_variant = 0, shadow_variant = 0;
+    int extend_grid_v[4] = {0, 0, 0, 0}, shadow_grid_v[4] = {0, 0, 0, 0};
     int resident_blocks_256 = 0;
 };
 

@@ -77,6 +77,11 @@ class pt_stats(C.Structure):
     ]
 
 
+class pt_tuning(C.Structure):
+    _fields_ = [("extend_variant", C.c_int32), ("shadow_variant", C.c_int32), ("extend_refill", C.c_int32),
+                ("shadow_refill", C.c_int32), ("min_tris", C.c_int32), ("frame_ms", C.c_float)]
+
+
 class pt_stage_stats(C.Structure):
     _fields_ = [("ms", C.c_float * 5), ("launches", C.c_int32 * 5)]
 
@@ -164,6 +169,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_trace_shadow.argtypes = [P, C.POINTER(pt_ray), _f, C.c_int32, _u8]
     lib.pt_bsdf_eval.argtypes = [P, _f, _f, _f, _f, C.c_int32, _f, _f]
     lib.pt_bsdf_sample.argtypes = [P, _f, _f, _f, C.POINTER(C.c_uint32), C.c_int32, _f, _f, _f]
+    lib.pt_autotune.argtypes = [P, C.c_int32, C.POINTER(pt_tuning)]
+    lib.pt_get_tuning.argtypes = [P, C.POINTER(pt_tuning)]
+    lib.pt_set_tuning.argtypes = [P, C.POINTER(pt_tuning)]
     lib.pt_set_stage_timing.argtypes = [P, C.c_int32]
     lib.pt_get_stage_stats.argtypes = [P, C.POINTER(pt_stage_stats)]
     lib.pt_get_stats.argtypes = [P, C.POINTER(pt_stats)]
@@ -172,7 +180,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
                  "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
                  "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
-                 "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing",
+                 "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune",
+                 "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
                  "pt_get_stage_stats", "pt_get_stats", "pt_last_error"):
         getattr(lib, name).restype = C.c_int
     if path is None:
@@ -185,7 +194,8 @@ HEADER_SYMBOLS = [
     "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_tile_noalloc",
     "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
     "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
-    "pt_bsdf_eval", "pt_bsdf_sample", "pt_set_stage_timing", "pt_get_stage_stats", "pt_get_stats",
+    "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune", "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
+    "pt_get_stage_stats", "pt_get_stats",
     "pt_last_error",
 ]
 

@@ -118,6 +118,25 @@ class GpuRenderer:
         self._ck(self.lib.pt_render_adjoint(self.ctx, first_pass, num_passes, fp(di), fp(g)))
         return g
 
+    TUNING_FIELDS = ("extend_variant", "shadow_variant", "extend_refill", "shadow_refill", "min_tris")
+
+    def autotune(self, num_passes: int = 2) -> dict:
+        t = capi.pt_tuning()
+        self._ck(self.lib.pt_autotune(self.ctx, num_passes, C.byref(t)))
+        return {**{k: getattr(t, k) for k in self.TUNING_FIELDS}, "frame_ms": t.frame_ms}
+
+    def tuning(self) -> dict:
+        t = capi.pt_tuning()
+        self._ck(self.lib.pt_get_tuning(self.ctx, C.byref(t)))
+        return {k: getattr(t, k) for k in self.TUNING_FIELDS}
+
+    def set_tuning(self, **kw):
+        t = capi.pt_tuning()
+        self._ck(self.lib.pt_get_tuning(self.ctx, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._ck(self.lib.pt_set_tuning(self.ctx, C.byref(t)))
+
     def set_stage_timing(self, on: bool):
         self._ck(self.lib.pt_set_stage_timing(self.ctx, 1 if on else 0))
 

@@ -287,6 +287,28 @@ int pt_bsdf_eval(pt_context* ctx, const float* records, const float* V, const fl
 int pt_bsdf_sample(pt_context* ctx, const float* records, const float* V, const float* N,
                    const uint32_t* seeds, int32_t n, float* L, float* f, float* pdf);
 
+/* Launch configuration of the wavefront integrator's traversal stages (no
+ * counterpart in the reference, whose shaders have none). */
+typedef struct pt_tuning {
+    int32_t extend_variant;  /* 0: 8 resident blocks of 128 (64 registers), scalar node test;
+                              * 1: 8 blocks, packed-FP32 node test; 2: 6 blocks (80 registers),
+                              * scalar; 3: 6 blocks, packed */
+    int32_t shadow_variant;  /* the same choices for the shadow-ray stage */
+    int32_t extend_refill;   /* idle lanes of a warp that trigger fetching new rays (1..32) */
+    int32_t shadow_refill;
+    int32_t min_tris;        /* lanes with triangles pending that run a triangle step (0: per lane) */
+    float   frame_ms;        /* pt_autotune: device time of the tuned frame */
+} pt_tuning;
+
+/* Autotuner: renders num_passes whole-frame passes (into a scratch
+ * accumulation, the context's is untouched) with candidate configurations,
+ * timing each stage with CUDA events, and keeps the fastest for this scene
+ * and frame size.  Coordinate descent: kernel variants (extend and shadow
+ * separately), refill thresholds (separately), then min_tris. */
+int pt_autotune(pt_context* ctx, int32_t num_passes, pt_tuning* result);
+int pt_get_tuning(pt_context* ctx, pt_tuning* tuning);
+int pt_set_tuning(pt_context* ctx, const pt_tuning* tuning);
+
 /* Per-stage device time of the wavefront integrator (no counterpart in the
  * reference; a profiling aid).  With stage timing on, each wavefront launch
  * of a render call is bracketed by CUDA events on the context's stream and
