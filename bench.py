@@ -18,7 +18,7 @@ segments), counted on the device.
              time of pt_render_adjoint (gradient of 375 parameters, reusing
              the forward paths) over that of the forward render.
   compare    the megakernel on the same frame and timing rules (it gives the
-             same accumulation bit for bit, so equal RMSE): the
+             same accumulation up to last-bit rounding, so equal RMSE): the
              wavefront / megakernel ratio.
   roofline   HBM, for the dominant kernel (wf_extend on this workload): its
              algorithmic bytes (36 B per node visit + 60 B per triangle test
@@ -351,7 +351,7 @@ def main():
     rays_per_step = rays / (args.steps * world)
 
     # the other integrator on the same frame, same timing rules (the two give
-    # the same accumulation bit for bit on this scene, so equal RMSE)
+    # the same accumulation up to last-bit rounding, so equal RMSE)
     other = None
     if args.compare_steps > 0:
         other_name = "megakernel" if args.integrator == "wavefront" else "wavefront"

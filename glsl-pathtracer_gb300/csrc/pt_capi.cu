@@ -90,6 +90,8 @@ struct pt_context {
     DevBuf<int32_t> vidx;
     DevBuf<float4> verts, norms, mats, lights, env;
     DevBuf<float> cdf;
+    DevBuf<uchar4> tex;
+    int tex_w = 0, tex_h = 0, num_tex = 0;
     DevBuf<float4> accum;
     DevBuf<float4> snapshot;
     DevBuf<uchar4> ldr;
@@ -127,6 +129,8 @@ uint32_t option_flags(const pt_context* c) {
     if (o.enable_roughness_mollification) f |= F_MOLLIFY;
     if (o.enable_envmap && c->has_env && !o.enable_uniform_light) f |= F_ENVMAP;
     if (o.enable_volume_mis) f |= F_VOL_MIS;
+    if (o.opengl_normal_map) f |= F_OPENGL_NORMALMAP;
+    if (c->num_tex > 0) f |= F_TEXTURES;
     return f;
 }
 
@@ -149,6 +153,10 @@ Params make_params(const pt_context* c) {
     p.env_w = c->env_w;
     p.env_h = c->env_h;
     p.env_total = c->env_total;
+    p.tex = c->tex.p;
+    p.tex_w = c->tex_w;
+    p.tex_h = c->tex_h;
+    p.num_tex = c->num_tex;
     p.env_intensity = c->opts.envmap_intensity;
     p.env_rot = c->opts.envmap_rot / 360.0f;  // Renderer.cpp:778
     p.flags = option_flags(c);
@@ -272,12 +280,15 @@ uint32_t scene_flags_of(const float* mats, int nm, int nl) {
     return f;
 }
 
-int check_materials(const float* mats, int nm) {
+// Texture ids of a material (Material.h:87-119, texIDs at 24..27) index the
+// texture array; -1 is none.
+int check_materials(const float* mats, int nm, int num_tex) {
     for (int i = 0; i < nm; ++i)
         for (int k = 24; k < 28; ++k)
-            if ((int)mats[32 * i + k] >= 0)
-                return set_err(PT_ERR_UNSUPPORTED, "material " + std::to_string(i) +
-                                                       " uses a texture map; texture maps are not supported yet");
+            if ((int)mats[32 * i + k] >= num_tex)
+                return set_err(PT_ERR_INVALID_ARG, "material " + std::to_string(i) + " uses texture " +
+                                                       std::to_string((int)mats[32 * i + k]) + " of " +
+                                                       std::to_string(num_tex));
     return PT_OK;
 }
 
@@ -353,8 +364,9 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
         !d->normals_uvy || d->num_vertices <= 0 || !d->transforms || d->num_instances <= 0 || !d->materials ||
         d->num_materials <= 0 || d->num_lights < 0 || (d->num_lights > 0 && !d->lights))
         return set_err(PT_ERR_INVALID_ARG, "incomplete scene description");
-    if (d->num_textures > 0) return set_err(PT_ERR_UNSUPPORTED, "texture maps are not supported yet");
-    if (int rc = check_materials(d->materials, d->num_materials)) return rc;
+    if (d->num_textures < 0 || (d->num_textures > 0 && (!d->texture_maps || d->tex_width <= 0 || d->tex_height <= 0)))
+        return set_err(PT_ERR_INVALID_ARG, "invalid texture maps");
+    if (int rc = check_materials(d->materials, d->num_materials, d->num_textures)) return rc;
     for (int i = 0; i < d->num_lights; ++i) {
         int type = (int)d->lights[15 * i + 14];
         if (type < 0 || type > 2) return set_err(PT_ERR_INVALID_ARG, "unknown light type");
@@ -398,6 +410,16 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
             break;
         }
         if ((rc = upload_lights(c, d->lights, d->num_lights))) break;
+        if (d->num_textures > 0) {
+            c->tex_w = d->tex_width;
+            c->tex_h = d->tex_height;
+            c->num_tex = d->num_textures;
+            if ((e = c->tex.upload(d->texture_maps, (size_t)d->num_textures * d->tex_width * d->tex_height,
+                                   c->stream)) != cudaSuccess) {
+                rc = cuda_err(e, "texture maps");
+                break;
+            }
+        }
         if ((rc = upload_envmap(c, d->envmap_rgb, d->envmap_cdf, d->envmap_width, d->envmap_height,
                                 d->envmap_total_sum)))
             break;
@@ -421,6 +443,7 @@ int pt_destroy(pt_context* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->vidx.free(); c->verts.free();
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
+    c->tex.free();
     c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();
     wavefront_free(c->wf);
     c->timer.release();
@@ -471,7 +494,7 @@ int pt_update_instances(pt_context* c, const float* transforms, int32_t num_inst
         return set_err(PT_ERR_INVALID_ARG, "invalid instance update");
     if (materials) {
         if (num_materials <= 0) return set_err(PT_ERR_INVALID_ARG, "num_materials must be positive");
-        if (int rc = check_materials(materials, num_materials)) return rc;
+        if (int rc = check_materials(materials, num_materials, c->num_tex)) return rc;
     }
     c->version++;
     int rc = check_tlas_materials(tlas_nodes, num_tlas_nodes, materials ? num_materials : c->num_materials);
@@ -584,7 +607,7 @@ int pt_update_materials(pt_context* c, const float* materials, int32_t num_mater
     if (!c || !materials) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     if (num_materials != c->num_materials)
         return set_err(PT_ERR_INVALID_ARG, "pt_update_materials: the number of materials cannot change");
-    if (int rc = check_materials(materials, num_materials)) return rc;
+    if (int rc = check_materials(materials, num_materials, c->num_tex)) return rc;
     CK(cudaStreamSynchronize(c->stream));
     CK(c->mats.upload(materials, 8 * (size_t)num_materials, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -611,9 +634,9 @@ int pt_render_adjoint(pt_context* c, int32_t first_pass, int32_t num_passes, con
     if (!c || !d_image || !grad) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     if (first_pass < 0 || num_passes <= 0) return set_err(PT_ERR_INVALID_ARG, "invalid pass range");
     const uint32_t flags = option_flags(c);
-    if (flags & (F_MEDIUM | F_ALPHA_TEST | F_ENVMAP))
-        return set_err(PT_ERR_UNSUPPORTED,
-                       "pt_render_adjoint: media, alpha-tested materials and environment maps are not differentiated");
+    if (flags & (F_MEDIUM | F_ALPHA_TEST | F_ENVMAP | F_TEXTURES))
+        return set_err(PT_ERR_UNSUPPORTED, "pt_render_adjoint: media, alpha-tested materials, environment maps and "
+                                           "texture maps are not differentiated");
     RenderWork w;
     w.x0 = w.y0 = 0;
     w.w = c->opts.render_width;

@@ -39,6 +39,8 @@ enum : uint32_t {
     F_ENVMAP = 1u << 7,           // OPT_ENVMAP && !OPT_UNIFORM_LIGHT
     F_MEDIUM = 1u << 8,
     F_VOL_MIS = 1u << 9,
+    F_TEXTURES = 1u << 10,        // the scene has texture maps (texelFetch / texture() on the array)
+    F_OPENGL_NORMALMAP = 1u << 11,
 };
 
 // ------------------------------------------------------------------ float3

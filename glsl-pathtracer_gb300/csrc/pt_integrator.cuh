@@ -130,10 +130,18 @@ __device__ __forceinline__ void TraceClosest(const Params& P, const Ray& r, int 
 }
 
 // Shading attributes of a triangle hit (closest_hit.glsl:224-247).
-__device__ __forceinline__ void HitNormal(const Params& P, const HitRecord& hr, const Ray& r, V3& normal, V3& ffnormal) {
+// Texture coordinate and tangent frame of a triangle hit (closest_hit.glsl:
+// 227-263); filled only when the scene has texture maps.
+struct Surface {
+    float u = 0.0f, v = 0.0f;
+    V3 T = {0.0f, 0.0f, 0.0f}, B = {0.0f, 0.0f, 0.0f};
+};
+
+__device__ __forceinline__ void HitNormal(const Params& P, const HitRecord& hr, const Ray& r, V3& normal, V3& ffnormal,
+                                          Surface* surf = nullptr) {
     const int i0 = __ldg(P.vidx + 3 * hr.prim), i1 = __ldg(P.vidx + 3 * hr.prim + 1), i2 = __ldg(P.vidx + 3 * hr.prim + 2);
-    const V3 n0 = v3(__ldg(P.norms + i0)), n1 = v3(__ldg(P.norms + i1)), n2 = v3(__ldg(P.norms + i2));
-    V3 n = normalize(n0 * hr.w + n1 * hr.u + n2 * hr.v);  // bary = uvt.wxy
+    const float4 n0 = __ldg(P.norms + i0), n1 = __ldg(P.norms + i1), n2 = __ldg(P.norms + i2);
+    V3 n = normalize(v3(n0) * hr.w + v3(n1) * hr.u + v3(n2) * hr.v);  // bary = uvt.wxy
     if (hr.inst >= 0) {
         const float4* x = P.xf + 10 * hr.inst + 7;
         const float4 c0 = __ldg(x), c1 = __ldg(x + 1), c2 = __ldg(x + 2);
@@ -142,13 +150,65 @@ __device__ __forceinline__ void HitNormal(const Params& P, const HitRecord& hr, 
     }
     normal = normalize(n);
     ffnormal = dot(normal, r.direction) <= 0.0f ? normal : -normal;
+    if (surf && (P.flags & F_TEXTURES)) {
+        const float4 p0 = __ldg(P.verts + i0), p1 = __ldg(P.verts + i1), p2 = __ldg(P.verts + i2);
+        surf->u = p0.w * hr.w + p1.w * hr.u + p2.w * hr.v;
+        surf->v = n0.w * hr.w + n1.w * hr.u + n2.w * hr.v;
+        const V3 dP1 = v3(p1) - v3(p0), dP2 = v3(p2) - v3(p0);
+        const float du1 = p1.w - p0.w, dv1 = n1.w - n0.w, du2 = p2.w - p0.w, dv2 = n2.w - n0.w;
+        const float invdet = 1.0f / (du1 * dv2 - dv1 * du2);
+        V3 T = (dP1 * dv2 - dP2 * dv1) * invdet;
+        V3 B = (dP2 * du1 - dP1 * du2) * invdet;
+        if (hr.inst >= 0) {  // mat3(transform)
+            const float4* m = P.xf + 10 * hr.inst + 4;
+            const float4 c0 = __ldg(m), c1 = __ldg(m + 1), c2 = __ldg(m + 2);
+            T = v3(c0.x * T.x + c1.x * T.y + c2.x * T.z, c0.y * T.x + c1.y * T.y + c2.y * T.z,
+                   c0.z * T.x + c1.z * T.y + c2.z * T.z);
+            B = v3(c0.x * B.x + c1.x * B.y + c2.x * B.z, c0.y * B.x + c1.y * B.y + c2.y * B.z,
+                   c0.z * B.x + c1.z * B.y + c2.z * B.z);
+        }
+        surf->T = normalize(T);
+        surf->B = normalize(B);
+    }
 }
 
-// GetMaterial (pathtrace.glsl:25-115) without texture maps.
-__device__ __forceinline__ void GetMaterial(const Params& P, int matID, int depth, float prevRough, V3 normal,
-                                            const Ray& r, Material& mat, float& eta) {
+__device__ __forceinline__ V3 pow22(float4 t) { return v3(powf(t.x, 2.2f), powf(t.y, 2.2f), powf(t.z, 2.2f)); }
+
+// GetMaterial (pathtrace.glsl:25-115): the material record, its texture maps
+// (base colour and opacity, metallic-roughness, normal map -- which bends
+// normal / ffnormal -- and emission), roughness mollification, then ax / ay
+// and eta.
+__device__ __forceinline__ void GetMaterial(const Params& P, int matID, int depth, float prevRough, V3& normal,
+                                            V3& ffnormal, const Surface& sf, const Ray& r, Material& mat,
+                                            float& eta) {
     LoadMaterial(P.mats, matID, mat);
-    if ((P.flags & F_MOLLIFY) && depth > 0) mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
+    if (P.flags & F_TEXTURES) {
+        const float4 ids = __ldg(P.mats + 8 * matID + 6);  // baseColor, metallicRoughness, normalmap, emission
+        if ((int)ids.x >= 0) {
+            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.x);
+            mat.baseColor = mat.baseColor * pow22(t);
+            mat.opacity *= t.w;
+        }
+        if ((int)ids.y >= 0) {
+            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.y);
+            mat.metallic = t.z;
+            mat.roughness = fmaxf(t.y * t.y, 0.001f);
+        }
+        if ((int)ids.z >= 0) {
+            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.z);
+            V3 tn = v3(t.x, t.y, t.z);
+            if (P.flags & F_OPENGL_NORMALMAP) tn.y = 1.0f - tn.y;
+            tn = normalize(tn * 2.0f - v3(1.0f));
+            const V3 orig = normal;
+            normal = normalize(sf.T * tn.x + sf.B * tn.y + normal * tn.z);
+            ffnormal = dot(orig, r.direction) <= 0.0f ? normal : -normal;
+        }
+        if ((P.flags & F_MOLLIFY) && depth > 0)
+            mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
+        if ((int)ids.w >= 0) mat.emission = pow22(SampleTexArray(P, sf.u, sf.v, ids.w));
+    } else if ((P.flags & F_MOLLIFY) && depth > 0) {
+        mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
+    }
     FinishMaterial(mat);
     eta = dot(r.direction, normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
 }
@@ -201,11 +261,12 @@ static __device__ __noinline__ V3 EvalTransmittance(const Params& P, Ray r, Rng&
         TraceClosest(P, r, 0, hr, stack, cnt, true);
         if (!hr.hit || hr.isEmitter) break;
         V3 normal, ffnormal;
-        HitNormal(P, hr, r, normal, ffnormal);
+        Surface sf;
+        HitNormal(P, hr, r, normal, ffnormal, &sf);
         matID = hr.mat;
         Material mat;
         float eta;
-        GetMaterial(P, matID, 0, 0.0f, normal, r, mat, eta);
+        GetMaterial(P, matID, 0, 0.0f, normal, ffnormal, sf, r, mat, eta);
         bool alphatest = AlphaSkip(mat, rng);
         bool refractive = (1.0f - mat.metallic) * mat.specTrans > 0.0f;
         if (!(alphatest || refractive)) return v3(0.0f);
@@ -501,14 +562,15 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
     }
     const V3 fhp = ps.r.origin + ps.r.direction * hr.t;
     V3 normal = v3(0.0f), ffnormal = v3(0.0f);
+    Surface sf;
     if (hr.prim >= 0) {
-        HitNormal(P, hr, ps.r, normal, ffnormal);
+        HitNormal(P, hr, ps.r, normal, ffnormal, &sf);
         ps.matID = hr.mat;
     }
     Material mat;
     float eta;
     hook.material(ps, ps.prevRough);
-    GetMaterial(P, ps.matID, ps.depth, ps.prevRough, normal, ps.r, mat, eta);
+    GetMaterial(P, ps.matID, ps.depth, ps.prevRough, normal, ffnormal, sf, ps.r, mat, eta);
     ps.prevRough = mat.roughness;
     ps.radiance = ps.radiance + mat.emission * ps.throughput;
     if ((F & F_LIGHTS) && hr.isEmitter) {

@@ -36,6 +36,9 @@ struct Params {
     // environment map (RGB padded to float4) and its CDF
     const float4* env;
     const float* cdf;
+    // texture maps: num_tex RGBA8 layers of tex_w x tex_h (textureMapsArrayTex)
+    const uchar4* tex;
+    int tex_w, tex_h, num_tex;
     int env_w, env_h;
     float env_total, env_intensity, env_rot;
     // options

@@ -240,6 +240,43 @@ __device__ __forceinline__ V3 xform_point(const float4* __restrict__ xf, int ins
     return r;
 }
 
+// texture(textureMapsArrayTex, vec3(uv, layer)): bilinear, GL_REPEAT, texel
+// centres at (i + 0.5) / size, the layer rounded and clamped; RGBA8 / 255.
+__device__ __forceinline__ float4 SampleTexArray(const Params& P, float u, float v, float layerf) {
+    int layer = (int)floorf(layerf + 0.5f);
+    layer = min(max(layer, 0), P.num_tex - 1);
+    const int w = P.tex_w, h = P.tex_h;
+    const uchar4* base = P.tex + (size_t)layer * w * h;
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = x - fx, ay = y - fy;
+    auto wrap = [](long long i, int n) {
+        long long m = i % n;
+        return (int)(m < 0 ? m + n : m);
+    };
+    const long long ix = (long long)fx, iy = (long long)fy;
+    const int x0 = wrap(ix, w), x1 = wrap(ix + 1, w), y0 = wrap(iy, h), y1 = wrap(iy + 1, h);
+    const uchar4 t00 = __ldg(base + (size_t)y0 * w + x0), t10 = __ldg(base + (size_t)y0 * w + x1);
+    const uchar4 t01 = __ldg(base + (size_t)y1 * w + x0), t11 = __ldg(base + (size_t)y1 * w + x1);
+    auto lerp2 = [&](unsigned char a, unsigned char b, unsigned char c, unsigned char d) {
+        const float ta = (float)a / 255.0f, tb = (float)b / 255.0f, tc = (float)c / 255.0f, td = (float)d / 255.0f;
+        const float r0 = ta * (1.0f - ax) + tb * ax;
+        const float r1 = tc * (1.0f - ax) + td * ax;
+        return r0 * (1.0f - ay) + r1 * ay;
+    };
+    return make_float4(lerp2(t00.x, t10.x, t01.x, t11.x), lerp2(t00.y, t10.y, t01.y, t11.y),
+                       lerp2(t00.z, t10.z, t01.z, t11.z), lerp2(t00.w, t10.w, t01.w, t11.w));
+}
+
+// Texture coordinate of a point (barycentrics u, v, w) of triangle `prim`:
+// u from verticesUVX.w, v from normalsUVY.w (bary = uvt.wxy).
+__device__ __forceinline__ void TriTexCoord(const Params& P, int prim, float u, float v, float w, float& tu,
+                                            float& tv) {
+    const int i0 = __ldg(P.vidx + 3 * prim), i1 = __ldg(P.vidx + 3 * prim + 1), i2 = __ldg(P.vidx + 3 * prim + 2);
+    tu = __ldg(P.verts + i0).w * w + __ldg(P.verts + i1).w * u + __ldg(P.verts + i2).w * v;
+    tv = __ldg(P.norms + i0).w * w + __ldg(P.norms + i1).w * u + __ldg(P.norms + i2).w * v;
+}
+
 __device__ __forceinline__ void flag_status(int* status, int code) { atomicCAS(status, PT_OK, code); }
 
 // --------------------------------------------------------- state machine
@@ -336,8 +373,14 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                         if (!ALPHA) return TRAV_HIT;
                         const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
                         const int alphaMode = (int)ap.y;
-                        bool skip = alphaMode == ALPHA_MODE_MASK && ap.x < ap.z;
-                        if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > ap.x;
+                        float opacity = ap.x;
+                        if (P.flags & F_TEXTURES) {  // the base-colour map's alpha (layer 0 when none)
+                            float tu, tv;
+                            TriTexCoord(P, prim, u, v, w, tu, tv);
+                            opacity *= SampleTexArray(P, tu, tv, __ldg(P.mats + 8 * mat + 6).x).w;
+                        }
+                        bool skip = alphaMode == ALPHA_MODE_MASK && opacity < ap.z;
+                        if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > opacity;
                         if (!skip) return TRAV_HIT;
                     }
                 } else if (t < s.tmax || (s.prim >= 0 && (prim < s.prim || (prim == s.prim && inst < s.inst)))) {

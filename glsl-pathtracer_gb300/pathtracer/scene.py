@@ -106,6 +106,8 @@ class SceneData:
         if self.envmap_rgb is not None:
             arrays["envmap_rgb"] = self.envmap_rgb
             arrays["envmap_cdf"] = self.envmap_cdf
+        if self.texture_maps is not None and self.texture_maps.size:
+            arrays["texture_maps"] = self.texture_maps
         meta = dict(top_level_index=int(self.top_level_index), envmap_total_sum=float(self.envmap_total_sum),
                     options=self.options, camera=self.camera)
         np.savez_compressed(path, meta=np.frombuffer(json.dumps(meta).encode(), np.uint8), **arrays)
@@ -120,7 +122,8 @@ class SceneData:
             materials=z["materials"], lights=z["lights"],
             envmap_rgb=z["envmap_rgb"] if "envmap_rgb" in z else None,
             envmap_cdf=z["envmap_cdf"] if "envmap_cdf" in z else None,
-            envmap_total_sum=meta["envmap_total_sum"], options=meta["options"], camera=meta["camera"])
+            envmap_total_sum=meta["envmap_total_sum"], options=meta["options"], camera=meta["camera"],
+            texture_maps=z["texture_maps"] if "texture_maps" in z else None)
 
 
 def load_ref_dump(prefix: str) -> SceneData:

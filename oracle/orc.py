@@ -209,6 +209,7 @@ def variant_for(scene, options) -> str:
         (False, True, True, True, True, True): "volmis",
         (False, True, True, True, False, True): "vol",
         (True, True, True, True, True, True): "envvolmis",
+        (False, True, True, False, False, True): "alpha",
     }
     if key not in table:
         raise KeyError(f"no reference shader variant built for {key}")

@@ -9,6 +9,9 @@ Run in a container that has the reference source (path in REF below) after
                          compiled for the CPU (oracle/_ref/libref_glsl_<variant>.so)
   ref_bsdf.npz           reference DisneyEval on random shading states
   ref_closest.npz        reference ClosestHit (lights + BVH) on ray sets
+  ref_scene_textured.npz / ref_render_textured.npz
+                         a textured scene of this project's (every texture
+                         slot, alpha blend) rendered by the reference
 """
 from __future__ import annotations
 
@@ -96,7 +99,95 @@ def closest_rays(sd: SceneData, n: int, seed: int):
     return orc.rays_array(np.concatenate([o1, o2]).astype(np.float32), np.concatenate([d, d2]).astype(np.float32))
 
 
+# A textured scene of this project's own, rendered by the reference: the
+# quad and checker texture of the reference's teapot assets (loaded through
+# relative paths from a scratch directory) under every texture slot, an
+# alpha-blended textured veil, and a quad light.  Texture array 64 x 64.
+TEXTURED_SCENE = """renderer
+{{
+    resolution 64 48
+    maxdepth 3
+    tilewidth 32
+    tileheight 24
+    texarraywidth 64
+    texarrayheight 64
+}}
+camera
+{{
+    position 0 6 12
+    lookat 0 0 0
+    fov 45
+}}
+light
+{{
+    type quad
+    position -2 8 -2
+    v1 2 8 -2
+    v2 -2 8 2
+    emission 30 30 30
+}}
+material floor
+{{
+    albedotexture {a}/checker.png
+    metallicroughnesstexture {a}/checker.png
+    normaltexture {a}/checker.png
+    roughness 0.5
+}}
+material veil
+{{
+    albedotexture {a}/checker.png
+    alphamode blend
+    opacity 0.5
+}}
+material glow
+{{
+    color 0.8 0.8 0.8
+    emissiontexture {a}/checker.png
+}}
+mesh
+{{
+    file {a}/Mesh050.obj
+    material floor
+    scale 0.01 0.01 0.01
+}}
+mesh
+{{
+    file {a}/Mesh050.obj
+    material veil
+    scale 0.002 0.002 0.002
+    position 0 1 0
+}}
+mesh
+{{
+    file {a}/Mesh050.obj
+    material glow
+    scale 0.001 0.001 0.001
+    position 3 0.5 -3
+}}
+"""
+
+
+def textured_golden():
+    with tempfile.TemporaryDirectory() as td:
+        rel = os.path.relpath(os.path.join(REF, "assets", "teapot"), td)
+        path = os.path.join(td, "textured.scene")
+        with open(path, "w") as fh:
+            fh.write(TEXTURED_SCENE.format(a=rel))
+        orc.ref_dump_scene(path, os.path.join(td, "textured"))
+        sd = load_ref_dump(os.path.join(td, "textured"))
+    sd.save_npz(os.path.join(HERE, "ref_scene_textured.npz"))
+    o = sd.render_options()
+    variant = orc.variant_for(sd, o)
+    acc = orc.ref_render(variant, sd, o, sd.pt_camera(), 0, 4)
+    np.savez_compressed(os.path.join(HERE, "ref_render_textured.npz"), accum=acc, passes=4, width=64, height=48,
+                        tile_w=32, tile_h=24, variant=variant)
+    return float(acc[..., :3].mean())
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "textured":
+        print("textured golden written", textured_golden())
+        return
     if not orc.ref_available():
         raise SystemExit("oracle/_ref not built: run `make -C oracle ref` first")
     out = {}
@@ -141,6 +232,7 @@ def main():
         res[name] = dict(rays=rays, hit=hit, t=t, mat=mat, emitter=emi, normal=nrm)
     np.savez_compressed(os.path.join(HERE, "ref_closest.npz"),
                         **{f"{k}_{f}": v for k, r in res.items() for f, v in r.items()})
+    out["textured"] = textured_golden()
     print("golden fixtures written", out)
 
 

@@ -16,6 +16,7 @@ from conftest import golden, golden_scene
     ("cornell_box_orig", "ref_scene_cornell_box_orig.npz"),
     ("volume_cube", "ref_scene_volume_cube.npz"),
     ("cornell_c1_48", "scene_cornell_c1_48.npz"),
+    ("textured", "ref_scene_textured.npz"),
 ])
 def test_render_bit_exact_vs_reference_shaders(orc, name, scene_file):
     sd = golden_scene(scene_file)
