@@ -828,6 +828,7 @@ void tuning_out(const WavefrontTuning& t, float ms, pt_tuning* out) {
     out->extend_refill = t.extend_refill;
     out->shadow_refill = t.shadow_refill;
     out->min_tris = t.min_tris;
+    out->shade_variant = t.shade_variant;
     out->frame_ms = ms;
 }
 }  // namespace
@@ -917,6 +918,19 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
             if (rc) break;
             best.min_tris = mt;
         }
+        // 4. register budget of the plain surface shading stage
+        {
+            float bsh = 1e30f;
+            int vsh = best.shade_variant;
+            for (int v = 0; v < 3; ++v) {
+                WavefrontTuning t = best;
+                t.shade_variant = v;
+                if ((rc = measure(t, ms))) break;
+                if (ms[STAGE_SHADE] < bsh) { bsh = ms[STAGE_SHADE]; vsh = v; }
+            }
+            if (rc) break;
+            best.shade_variant = vsh;
+        }
         if ((rc = measure(best, ms))) break;
     } while (false);
     timer.release();
@@ -945,7 +959,7 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
     if (!c || !in) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     if (in->extend_variant < 0 || in->extend_variant > 3 || in->shadow_variant < 0 || in->shadow_variant > 3 ||
         in->extend_refill < 1 || in->extend_refill > 32 || in->shadow_refill < 1 || in->shadow_refill > 32 ||
-        in->min_tris < 0 || in->min_tris > 32)
+        in->min_tris < 0 || in->min_tris > 32 || in->shade_variant < 0 || in->shade_variant > 2)
         return set_err(PT_ERR_INVALID_ARG, "tuning value out of range");
     if (!c->wf_tuned) {
         CK(wavefront_default_tuning(c->wf_tuning, 128));
@@ -956,6 +970,7 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
     c->wf_tuning.extend_refill = in->extend_refill;
     c->wf_tuning.shadow_refill = in->shadow_refill;
     c->wf_tuning.min_tris = in->min_tris;
+    c->wf_tuning.shade_variant = in->shade_variant;
     return PT_OK;
 }
 

@@ -298,8 +298,8 @@ __device__ __forceinline__ void adj_flush(const AdjView& A, const float* sgrad) 
         if (sgrad[k] != 0.0f) atomicAdd(A.grad + k, sgrad[k]);
 }
 
-template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false>
-__global__ void __launch_bounds__(128) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
+template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
     uint2 stack[INLINE ? kStackSize : 1];
     extern __shared__ float sgrad[];
     float* acc = nullptr;
@@ -540,7 +540,20 @@ cudaError_t launch_shade(const Params& p, const WfView& v, int in, int grid, int
     return cudaGetLastError();
 }
 
-cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
+// The plain surface shade (no media, no environment map, deferred shadow
+// rays) in three register budgets: unbounded, 80 (6 blocks) and 64 (8).
+cudaError_t launch_shade_plain(const Params& p, const WfView& v, int in, int variant, const int grids[3], int block,
+                               cudaStream_t s) {
+    switch (variant) {
+        case 1: wf_shade<0, false, false, false, 6><<<grids[1], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
+        case 2: wf_shade<0, false, false, false, 8><<<grids[2], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
+        default: wf_shade<0, false, false><<<grids[0], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s,
+                           int variant = 0, const int* grids = nullptr) {
     const int medium = (p.flags & F_MEDIUM) ? ((p.flags & F_VOL_MIS) ? 2 : 1) : 0;
     const bool env = (p.flags & F_ENVMAP) != 0;
     // AnyHit draws random numbers for alpha-tested materials without media
@@ -548,7 +561,10 @@ cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, i
     // the shadow rays inline so every path draws the reference's sequence
     const bool inl = medium == 2 || ((p.flags & F_ALPHA_TEST) && medium == 0);
     switch ((medium * 2 + (env ? 1 : 0)) * 2 + (inl ? 1 : 0)) {
-        case 0: return launch_shade<0, false, false>(p, v, in, grid, block, s);
+        case 0: {
+            const int g3[3] = {grid, grids ? grids[1] : grid, grids ? grids[2] : grid};
+            return launch_shade_plain(p, v, in, grids ? variant : 0, g3, block, s);
+        }
         case 1: return launch_shade<0, false, true>(p, v, in, grid, block, s);
         case 2: return launch_shade<0, true, false>(p, v, in, grid, block, s);
         case 3: return launch_shade<0, true, true>(p, v, in, grid, block, s);
@@ -742,7 +758,10 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
         if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, in, t, s); })) != cudaSuccess)
             return e;
         if ((e = timed(timer, STAGE_SHADE, s,
-                       [&] { return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
+                       [&] {
+                           return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant,
+                                                 t.shade_grid_v);
+                       })) != cudaSuccess)
             return e;
         if ((e = timed(timer, STAGE_SHADOW, s,
                        [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s); })) != cudaSuccess)
@@ -813,7 +832,9 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
                 if (count == 0) break;
                 const int in = it & 1;
                 if ((e = launch_extend(p, v, in, t, s)) != cudaSuccess) return e;
-                if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s)) != cudaSuccess) return e;
+                if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant, t.shade_grid_v)) !=
+                    cudaSuccess)
+                    return e;
                 if ((e = launch_shadow<false>(p, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
                 nl += 3;
             }
@@ -879,6 +900,14 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     b_ext = t.extend_grid_v[0] / sms;
     b_shadow = t.shadow_grid_v[0] / sms;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_shade, wf_shade<0, false, false>, block, 0);
+    {
+        int b6 = 0, b8 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b6, wf_shade<0, false, false, false, 6>, block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b8, wf_shade<0, false, false, false, 8>, block, 0);
+        t.shade_grid_v[0] = sms * std::max(1, b_shade);
+        t.shade_grid_v[1] = sms * std::max(1, b6);
+        t.shade_grid_v[2] = sms * std::max(1, b8);
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b256, wf_resolve, 256, 0);
     t.extend_block = t.shade_block = t.shadow_block = block;
     t.extend_grid = sms * std::max(1, b_ext);
@@ -896,6 +925,10 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     if (const char* r = std::getenv("PT_WAVEFRONT_VARIANT")) {
         const int v = std::atoi(r);
         if (v >= 0 && v < 4) t.extend_variant = t.shadow_variant = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_SHADE_VARIANT")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v < 3) t.shade_variant = v;
     }
     return cudaSuccess;
 }

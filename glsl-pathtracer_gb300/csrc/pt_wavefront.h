@@ -43,6 +43,10 @@ struct WavefrontTuning {
     // persistent grid of each variant fills the GPU
     int extend_variant = 0, shadow_variant = 0;
     int extend_grid_v[4] = {0, 0, 0, 0}, shadow_grid_v[4] = {0, 0, 0, 0};
+    // the plain surface shade stage: 0 = no register bound, 1 = 80 registers
+    // (6 blocks), 2 = 64 registers (8 blocks)
+    int shade_variant = 0;
+    int shade_grid_v[3] = {0, 0, 0};
     int resident_blocks_256 = 0;
 };
 

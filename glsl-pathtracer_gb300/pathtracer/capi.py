@@ -79,7 +79,8 @@ class pt_stats(C.Structure):
 
 class pt_tuning(C.Structure):
     _fields_ = [("extend_variant", C.c_int32), ("shadow_variant", C.c_int32), ("extend_refill", C.c_int32),
-                ("shadow_refill", C.c_int32), ("min_tris", C.c_int32), ("frame_ms", C.c_float)]
+                ("shadow_refill", C.c_int32), ("min_tris", C.c_int32), ("shade_variant", C.c_int32),
+                ("frame_ms", C.c_float)]
 
 
 class pt_stage_stats(C.Structure):

@@ -118,7 +118,8 @@ class GpuRenderer:
         self._ck(self.lib.pt_render_adjoint(self.ctx, first_pass, num_passes, fp(di), fp(g)))
         return g
 
-    TUNING_FIELDS = ("extend_variant", "shadow_variant", "extend_refill", "shadow_refill", "min_tris")
+    TUNING_FIELDS = ("extend_variant", "shadow_variant", "extend_refill", "shadow_refill", "min_tris",
+                     "shade_variant")
 
     def autotune(self, num_passes: int = 2) -> dict:
         t = capi.pt_tuning()

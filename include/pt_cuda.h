@@ -297,6 +297,7 @@ typedef struct pt_tuning {
     int32_t extend_refill;   /* idle lanes of a warp that trigger fetching new rays (1..32) */
     int32_t shadow_refill;
     int32_t min_tris;        /* lanes with triangles pending that run a triangle step (0: per lane) */
+    int32_t shade_variant;   /* surface shading stage: 0 unbounded registers, 1 at most 80, 2 at most 64 */
     float   frame_ms;        /* pt_autotune: device time of the tuned frame */
 } pt_tuning;
 
@@ -304,7 +305,8 @@ typedef struct pt_tuning {
  * accumulation, the context's is untouched) with candidate configurations,
  * timing each stage with CUDA events, and keeps the fastest for this scene
  * and frame size.  Coordinate descent: kernel variants (extend and shadow
- * separately), refill thresholds (separately), then min_tris. */
+ * separately), refill thresholds (separately), min_tris, then the shading
+ * stage's register budget. */
 int pt_autotune(pt_context* ctx, int32_t num_passes, pt_tuning* result);
 int pt_get_tuning(pt_context* ctx, pt_tuning* tuning);
 int pt_set_tuning(pt_context* ctx, const pt_tuning* tuning);

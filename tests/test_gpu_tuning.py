@@ -25,7 +25,7 @@ def test_every_configuration_gives_the_same_image(ptlib, name):
         ref = None
         for variant, refill, min_tris in itertools.product(range(4), (1, 8, 32), (0, 8)):
             r.set_tuning(extend_variant=variant, shadow_variant=3 - variant, extend_refill=refill,
-                         shadow_refill=refill, min_tris=min_tris)
+                         shadow_refill=refill, min_tris=min_tris, shade_variant=variant % 3)
             r.clear()
             r.render_passes(0, 3)
             a = r.accum()
