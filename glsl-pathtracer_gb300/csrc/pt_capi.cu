@@ -15,6 +15,7 @@
 #include "bvh8.h"
 #include "pt_device.cuh"
 #include "pt_params.h"
+#include "pt_bvh_gpu.h"
 #include "pt_grad.cuh"
 #include "pt_wavefront.h"
 
@@ -112,6 +113,10 @@ struct pt_context {
         RenderWork w{};
         uint64_t version = 0;
     } fwd;
+    // the BVH built on the GPU (pt_create_gpu_bvh): meshes and instances
+    bool gpu_bvh = false;
+    std::vector<int> mesh_tri_offset, inst_mesh, inst_material;
+    float gpu_build_ms = 0.0f;
     // adjoint buffers
     DevBuf<float4> adj_v, adj_le;
     DevBuf<float> adj_dimage, adj_grad;
@@ -356,11 +361,84 @@ int pt_last_error(char* buf, size_t size) {
     return PT_OK;
 }
 
-int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** out) {
+}  // extern "C"
+
+namespace {
+// The BVH of a context built on the GPU from its meshes (pt_bvh_gpu.cu);
+// the previous arrays are replaced only when the build succeeds.
+int gpu_rebuild(pt_context* c, const float* transforms) {
+    GpuBuildInput in;
+    in.verts = c->verts.p;
+    in.vidx = c->vidx.p;
+    in.mesh_tri_offset = c->mesh_tri_offset.data();
+    in.num_meshes = (int)c->mesh_tri_offset.size() - 1;
+    in.transforms = transforms;
+    in.inst_mesh = c->inst_mesh.data();
+    in.inst_material = c->inst_material.data();
+    in.num_instances = (int)c->inst_mesh.size();
+    GpuBvh g;
+    std::string err;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    cudaError_t e = gpu_build_bvh(in, g, c->stream, err);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        g.release();
+        return set_err(e == cudaErrorMemoryAllocation ? PT_ERR_OUT_OF_MEMORY : PT_ERR_INVALID_ARG,
+                       "GPU BVH build: " + (err.empty() ? std::string(cudaGetErrorString(e)) : err));
+    }
+    if (g.tlas_depth + g.blas_depth + 3 > kStackSize) {
+        g.release();
+        return set_err(PT_ERR_UNSUPPORTED, "GPU-built BVH deeper than the traversal stack");
+    }
+    c->nodes.free();
+    c->tris.free();
+    c->insts.free();
+    c->nodes.p = g.nodes;
+    c->nodes.n = g.num_nodes;
+    c->tris.p = g.tris;
+    c->tris.n = g.num_tris;
+    c->insts.p = g.insts;
+    c->insts.n = g.num_insts;
+    c->bvh.tlas_root = g.tlas_root;
+    c->bvh.tlas_first_node = g.tlas_first_node;
+    c->bvh.blas_depth = g.blas_depth;
+    c->bvh.tlas_depth = g.tlas_depth;
+    c->bvh.num_nodes = g.num_nodes;
+    c->bvh.num_tris = g.num_tris;
+    c->bvh.num_inst_refs = g.num_insts;
+    c->gpu_build_ms = ms;
+    return PT_OK;
+}
+
+int create(const pt_scene_desc* d, const pt_mesh_desc* meshes, const pt_render_options* o, pt_context** out) {
     if (!d || !out) return set_err(PT_ERR_INVALID_ARG, "scene or output pointer is NULL");
     *out = nullptr;
     if (int rc = check_options(o)) return rc;
-    if (!d->bvh_nodes || d->num_bvh_nodes <= 0 || !d->vert_indices || d->num_tris < 0 || !d->vertices_uvx ||
+    if (meshes) {
+        if (!meshes->mesh_tri_offset || meshes->num_meshes <= 0 || !meshes->instance_mesh ||
+            !meshes->instance_material)
+            return set_err(PT_ERR_INVALID_ARG, "incomplete mesh description");
+        if (meshes->mesh_tri_offset[0] != 0 || meshes->mesh_tri_offset[meshes->num_meshes] != d->num_tris)
+            return set_err(PT_ERR_INVALID_ARG, "mesh triangle offsets must run from 0 to num_tris");
+        for (int m = 0; m < meshes->num_meshes; ++m)
+            if (meshes->mesh_tri_offset[m + 1] < meshes->mesh_tri_offset[m])
+                return set_err(PT_ERR_INVALID_ARG, "mesh triangle offsets must not decrease");
+        for (int i = 0; i < d->num_instances; ++i) {
+            if (meshes->instance_mesh[i] < 0 || meshes->instance_mesh[i] >= meshes->num_meshes)
+                return set_err(PT_ERR_INVALID_ARG, "instance mesh index out of range");
+            if (meshes->instance_material[i] < 0 || meshes->instance_material[i] >= d->num_materials)
+                return set_err(PT_ERR_INVALID_ARG, "instance material index out of range");
+        }
+    }
+    if ((!meshes && (!d->bvh_nodes || d->num_bvh_nodes <= 0)) || !d->vert_indices || d->num_tris < 0 || !d->vertices_uvx ||
         !d->normals_uvy || d->num_vertices <= 0 || !d->transforms || d->num_instances <= 0 || !d->materials ||
         d->num_materials <= 0 || d->num_lights < 0 || (d->num_lights > 0 && !d->lights))
         return set_err(PT_ERR_INVALID_ARG, "incomplete scene description");
@@ -384,23 +462,30 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
             rc = cuda_err(e, "cudaEventCreate");
             break;
         }
-        char msg[512] = {0};
-        rc = ptgb_build_wide(d->bvh_nodes, d->num_bvh_nodes, d->top_level_index, d->vert_indices, d->num_tris,
-                             d->vertices_uvx, d->num_vertices, d->transforms, d->num_instances, &c->bvh, msg,
-                             sizeof msg);
-        if (rc) { set_err(rc, std::string("BVH: ") + msg); break; }
-        if ((rc = check_tlas_materials(d->bvh_nodes + 9 * (size_t)d->top_level_index,
-                                       d->num_bvh_nodes - d->top_level_index, d->num_materials)))
-            break;
-        c->bin_nodes.assign(d->bvh_nodes, d->bvh_nodes + 9 * (size_t)d->num_bvh_nodes);
-        c->top_level_index = d->top_level_index;
+        if (!meshes) {
+            char msg[512] = {0};
+            rc = ptgb_build_wide(d->bvh_nodes, d->num_bvh_nodes, d->top_level_index, d->vert_indices, d->num_tris,
+                                 d->vertices_uvx, d->num_vertices, d->transforms, d->num_instances, &c->bvh, msg,
+                                 sizeof msg);
+            if (rc) { set_err(rc, std::string("BVH: ") + msg); break; }
+            if ((rc = check_tlas_materials(d->bvh_nodes + 9 * (size_t)d->top_level_index,
+                                           d->num_bvh_nodes - d->top_level_index, d->num_materials)))
+                break;
+            c->bin_nodes.assign(d->bvh_nodes, d->bvh_nodes + 9 * (size_t)d->num_bvh_nodes);
+            c->top_level_index = d->top_level_index;
+        } else {
+            c->gpu_bvh = true;
+            c->mesh_tri_offset.assign(meshes->mesh_tri_offset, meshes->mesh_tri_offset + meshes->num_meshes + 1);
+            c->inst_mesh.assign(meshes->instance_mesh, meshes->instance_mesh + d->num_instances);
+            c->inst_material.assign(meshes->instance_material, meshes->instance_material + d->num_instances);
+        }
         c->num_tris = d->num_tris;
         c->num_vertices = d->num_vertices;
         c->num_materials = d->num_materials;
         c->num_instances = d->num_instances;
         c->num_lights = d->num_lights;
         c->scene_flags = scene_flags_of(d->materials, d->num_materials, d->num_lights);
-        if ((rc = upload_bvh(c))) break;
+        if (!meshes && (rc = upload_bvh(c))) break;
         if ((rc = upload_instances(c, d->transforms, d->num_instances))) break;
         if ((e = c->vidx.upload(d->vert_indices, 3 * (size_t)d->num_tris, c->stream)) != cudaSuccess ||
             (e = c->verts.upload(d->vertices_uvx, d->num_vertices, c->stream)) != cudaSuccess ||
@@ -409,6 +494,7 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
             rc = cuda_err(e, "scene upload");
             break;
         }
+        if (meshes && (rc = gpu_rebuild(c, d->transforms))) break;
         if ((rc = upload_lights(c, d->lights, d->num_lights))) break;
         if (d->num_textures > 0) {
             c->tex_w = d->tex_width;
@@ -435,6 +521,39 @@ int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** o
         return rc;
     }
     *out = c;
+    return PT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pt_create(const pt_scene_desc* d, const pt_render_options* o, pt_context** out) {
+    return create(d, nullptr, o, out);
+}
+
+int pt_create_gpu_bvh(const pt_scene_desc* d, const pt_mesh_desc* meshes, const pt_render_options* o,
+                      pt_context** out) {
+    if (!meshes) return set_err(PT_ERR_INVALID_ARG, "mesh description is NULL");
+    return create(d, meshes, o, out);
+}
+
+int pt_update_transforms(pt_context* c, const float* transforms, int32_t num_instances) {
+    if (!c || !transforms) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    if (!c->gpu_bvh) return set_err(PT_ERR_INVALID_ARG, "pt_update_transforms needs a context from pt_create_gpu_bvh");
+    if (num_instances != (int)c->inst_mesh.size())
+        return set_err(PT_ERR_INVALID_ARG, "the number of instances cannot change");
+    CK(cudaStreamSynchronize(c->stream));
+    if (int rc = gpu_rebuild(c, transforms)) return rc;
+    if (int rc = upload_instances(c, transforms, num_instances)) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    c->version++;
+    c->fwd.valid = false;
+    return PT_OK;
+}
+
+int pt_gpu_build_ms(pt_context* c, float* ms) {
+    if (!c || !ms) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    *ms = c->gpu_build_ms;
     return PT_OK;
 }
 

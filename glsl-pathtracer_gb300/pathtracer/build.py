@@ -19,7 +19,7 @@ LIB = os.path.join(CSRC, "libptgb.so")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
-CU_SOURCES = ["pt_kernels.cu", "pt_wavefront.cu", "pt_capi.cu"]
+CU_SOURCES = ["pt_kernels.cu", "pt_wavefront.cu", "pt_capi.cu", "pt_bvh_gpu.cu"]
 CPP_SOURCES = ["bvh8_build.cpp", "cuda_renderer.cpp"]
 
 

@@ -40,6 +40,11 @@ class pt_scene_desc(C.Structure):
     ]
 
 
+class pt_mesh_desc(C.Structure):
+    _fields_ = [("mesh_tri_offset", _i), ("num_meshes", C.c_int32), ("instance_mesh", _i),
+                ("instance_material", _i)]
+
+
 class pt_render_options(C.Structure):
     _fields_ = [
         ("render_width", C.c_int32), ("render_height", C.c_int32),
@@ -149,6 +154,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib = C.CDLL(p)
     P = C.c_void_p
     lib.pt_create.argtypes = [C.POINTER(pt_scene_desc), C.POINTER(pt_render_options), C.POINTER(P)]
+    lib.pt_create_gpu_bvh.argtypes = [C.POINTER(pt_scene_desc), C.POINTER(pt_mesh_desc),
+                                      C.POINTER(pt_render_options), C.POINTER(P)]
+    lib.pt_update_transforms.argtypes = [P, _f, C.c_int32]
+    lib.pt_gpu_build_ms.argtypes = [P, _f]
     lib.pt_destroy.argtypes = [P]
     lib.pt_set_stream.argtypes = [P, P]
     lib.pt_set_camera.argtypes = [P, C.POINTER(pt_camera)]
@@ -177,7 +186,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_get_stage_stats.argtypes = [P, C.POINTER(pt_stage_stats)]
     lib.pt_get_stats.argtypes = [P, C.POINTER(pt_stats)]
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
-    for name in ("pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
+    for name in ("pt_create", "pt_create_gpu_bvh", "pt_update_transforms", "pt_gpu_build_ms", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
                  "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
                  "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
@@ -191,7 +200,7 @@ def load_library(path: str | None = None) -> C.CDLL:
 
 
 HEADER_SYMBOLS = [
-    "pt_create", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
+    "pt_create", "pt_create_gpu_bvh", "pt_update_transforms", "pt_gpu_build_ms", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
     "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_tile_noalloc",
     "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
     "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",

@@ -18,14 +18,34 @@ HIT_DTYPE = np.dtype([("t", np.float32), ("u", np.float32), ("v", np.float32), (
 
 
 class GpuRenderer:
-    def __init__(self, scene: SceneData, options: capi.pt_render_options | None = None, **overrides):
+    def __init__(self, scene: SceneData, options: capi.pt_render_options | None = None, gpu_bvh: bool = False,
+                 **overrides):
+        """gpu_bvh: build the BVH on the GPU (pt_create_gpu_bvh) from the
+        scene's meshes instead of collapsing its flattened binary BVH."""
         self.lib = capi.load_library()
         self.scene = scene
         self.options = options if options is not None else scene.render_options(**overrides)
         self._desc = scene.desc()
         self.ctx = C.c_void_p()
-        capi.check(self.lib, self.lib.pt_create(C.byref(self._desc), C.byref(self.options), C.byref(self.ctx)))
+        if gpu_bvh:
+            off, im, mat = scene.mesh_desc()
+            self._mesh_arrays = (off, im, mat)
+            ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+            self._mesh = capi.pt_mesh_desc(ip(off), len(off) - 1, ip(im), ip(mat))
+            capi.check(self.lib, self.lib.pt_create_gpu_bvh(C.byref(self._desc), C.byref(self._mesh),
+                                                            C.byref(self.options), C.byref(self.ctx)))
+        else:
+            capi.check(self.lib, self.lib.pt_create(C.byref(self._desc), C.byref(self.options), C.byref(self.ctx)))
         self.set_camera(scene.pt_camera())
+
+    def update_transforms(self, transforms: np.ndarray):
+        t = np.ascontiguousarray(transforms, np.float32)
+        self._ck(self.lib.pt_update_transforms(self.ctx, t.ctypes.data_as(C.POINTER(C.c_float)), t.shape[0]))
+
+    def gpu_build_ms(self) -> float:
+        ms = C.c_float()
+        self._ck(self.lib.pt_gpu_build_ms(self.ctx, C.byref(ms)))
+        return ms.value
 
     # ------------------------------------------------------------------
     @property

@@ -98,6 +98,48 @@ class SceneData:
         return capi.make_camera(c["position"], c["up"], c["right"], c["forward"], c["fov"],
                                 c.get("focal_dist", 0.1), c.get("aperture", 0.0))
 
+    def mesh_desc(self):
+        """Meshes and instances for pt_create_gpu_bvh, recovered from the
+        flattened BVH: each TLAS leaf gives an instance's BLAS root and
+        material, each BLAS its (contiguous) triangle range.  Returns the
+        arrays (mesh_tri_offset, instance_mesh, instance_material)."""
+        bn = self.bvh_nodes
+        top = int(self.top_level_index)
+        inst_root = {}
+        inst_mat = {}
+        for i in range(top, bn.shape[0]):
+            if bn[i, 8] < 0:
+                inst = int(-bn[i, 8]) - 1
+                inst_root[inst] = int(bn[i, 6])
+                inst_mat[inst] = int(bn[i, 7])
+        ranges = {}
+        for root in set(inst_root.values()):
+            lo, hi, stack = None, None, [root]
+            while stack:
+                b = stack.pop()
+                if bn[b, 8] == 0:
+                    stack += [int(bn[b, 6]), int(bn[b, 7])]
+                elif bn[b, 8] > 0 and int(bn[b, 7]) > 0:
+                    f, c = int(bn[b, 6]), int(bn[b, 7])
+                    lo = f if lo is None else min(lo, f)
+                    hi = f + c if hi is None else max(hi, f + c)
+            ranges[root] = (lo or 0, hi or 0)
+        starts = sorted(set(r for r in ranges.values()))
+        offsets, mesh_of_range = [0], {}
+        for lo, hi in starts:
+            if lo > offsets[-1]:
+                offsets.append(lo)  # triangles no instance uses: a mesh of their own
+            if lo < offsets[-1]:
+                raise ValueError("BLAS triangle ranges overlap")
+            mesh_of_range[(lo, hi)] = len(offsets) - 1
+            offsets.append(hi)
+        if offsets[-1] < self.num_tris:
+            offsets.append(self.num_tris)
+        n = self.transforms.shape[0]
+        inst_mesh = np.array([mesh_of_range[ranges[inst_root[i]]] for i in range(n)], np.int32)
+        inst_material = np.array([inst_mat[i] for i in range(n)], np.int32)
+        return np.array(offsets, np.int32), inst_mesh, inst_material
+
     # ------------------------------------------------------------------
     def save_npz(self, path: str):
         arrays = dict(bvh_nodes=self.bvh_nodes, vert_indices=self.vert_indices, vertices_uvx=self.vertices_uvx,

@@ -154,6 +154,32 @@ typedef struct pt_context pt_context;
 int pt_create(const pt_scene_desc* scene, const pt_render_options* options,
               pt_context** out_ctx);
 
+/* Meshes and instances as GLSLPT::Scene holds them before ProcessScene
+ * builds the BVH (src/core/Scene.h:88-102, Mesh.h:52-70): mesh m owns the
+ * triangles [mesh_tri_offset[m], mesh_tri_offset[m+1]) of vert_indices
+ * (ProcessScene's concatenation order, Scene.cpp:229-252). */
+typedef struct pt_mesh_desc {
+    const int32_t* mesh_tri_offset;    /* num_meshes + 1 offsets */
+    int32_t        num_meshes;
+    const int32_t* instance_mesh;      /* MeshInstance::meshID, one per scene instance */
+    const int32_t* instance_material;  /* MeshInstance::materialID */
+} pt_mesh_desc;
+
+/* Replaces: the BVH builds of Scene::ProcessScene (per-mesh RadeonRays SBVH,
+ * the TLAS and BvhTranslator, src/core/Scene.cpp:148-252) with a build on
+ * the GPU (LBVH + 8-wide collapse): like pt_create, but scene->bvh_nodes
+ * is ignored and may be NULL. */
+int pt_create_gpu_bvh(const pt_scene_desc* scene, const pt_mesh_desc* meshes,
+                      const pt_render_options* options, pt_context** out_ctx);
+
+/* Replaces: Scene::RebuildInstances + the TLAS upload of Renderer::Update
+ * (Scene.cpp:200-214, Renderer.cpp:647-663) for a context from
+ * pt_create_gpu_bvh: new instance transforms, the BVH rebuilt on the GPU. */
+int pt_update_transforms(pt_context* ctx, const float* transforms, int32_t num_instances);
+
+/* Device time of the last GPU BVH build (ms). */
+int pt_gpu_build_ms(pt_context* ctx, float* ms);
+
 /* Replaces: Renderer::~Renderer (src/core/Renderer.cpp:89-133). */
 int pt_destroy(pt_context* ctx);
 
