@@ -17,6 +17,11 @@ segments), counted on the device.
              in 32 materials + 4 lights, 512x512, 16 spp, depth 6): device
              time of pt_render_adjoint (gradient of 375 parameters, reusing
              the forward paths) over that of the forward render.
+  batch      64 jobs of uneven size (icosphere scenes of 10k-1M triangles,
+             128^2-1024^2, 1-64 spp, depth 4-12) in one pt_batch_render per
+             step: aggregate Mrays/s from the library's events around the
+             batch, p50/p99 of the jobs' completion times (device global
+             timer), and the same jobs rendered one after another.
   compare    the megakernel on the same frame and timing rules (it gives the
              same accumulation up to last-bit rounding, so equal RMSE): the
              wavefront / megakernel ratio.
@@ -258,6 +263,94 @@ def adjoint_bench(steps, stream, flush):
             "grad_finite": bool(np.isfinite(g).all())}
 
 
+BATCH_WORKLOAD = ("batched wavefront: 64 jobs, each the icosphere scene (16 Disney materials, one sphere light) "
+                  "at 10k-1M triangles (log-uniform, seed 3), resolution from {128^2,256^2,512^2,1024^2}, spp "
+                  "from {1,4,16,64}, depth 4-12; one pt_batch_render (CUDA graph) per step")
+
+
+def batch_jobs(n=64, seed=3):
+    """(freq, resolution, spp, depth) per job; triangles = 20 freq^2."""
+    import math
+    rng = np.random.RandomState(seed)
+    jobs = []
+    for _ in range(n):
+        tris = math.exp(rng.uniform(math.log(1e4), math.log(1e6)))
+        freq = max(2, int(round(math.sqrt(tris / 20.0))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.choice([1, 4, 16, 64]))
+        depth = int(rng.randint(4, 13))
+        jobs.append((freq, res, spp, depth))
+    return jobs
+
+
+def _batch_scene(args):
+    from pathtracer import scenes
+    j, (freq, res, spp, depth) = args
+    return scenes.icosphere_scene(freq=freq, width=res, height=res, max_depth=depth, seed=1 + j, tile=res)
+
+
+def batch_bench(steps, flush, n_jobs=64, sequential=True):
+    """The 64-job batch: per-job completion times (p50/p99) and aggregate
+    Mrays/s from the library's events around each pt_batch_render; beside it
+    the same jobs rendered one after another on their own contexts."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import torch
+    from pathtracer import capi
+    from pathtracer.renderer import GpuBatch, GpuRenderer
+    jobs = batch_jobs(n_jobs)
+    t0 = time.perf_counter()
+    with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
+                                mp_context=mp.get_context("spawn")) as ex:
+        scenes_ = list(ex.map(_batch_scene, enumerate(jobs)))
+    setup_s = time.perf_counter() - t0
+    rs = [GpuRenderer(sd) for sd in scenes_]
+    for r in rs:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+    big = max(range(n_jobs), key=lambda j: jobs[j][0])
+    tuning = rs[big].autotune(2)
+    spp = [jb[2] for jb in jobs]
+    paths = sum(jb[1] * jb[1] * jb[2] for jb in jobs)
+    res = {"workload": BATCH_WORKLOAD, "jobs": n_jobs, "paths_per_step": paths,
+           "tris": [20 * jb[0] ** 2 for jb in jobs], "tuning": tuning, "scene_setup_s": setup_s}
+    with GpuBatch(rs) as b:
+        lat, ms, rays, launches = [], [], 0, 0
+        for k in range(steps + 1):  # the first is warm-up
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize()
+            job_ms = b.render([spp[j] * k for j in range(n_jobs)], spp)
+            st = b.stats()
+            if st["status"] != 0:
+                raise RuntimeError(f"batch kernel status {st['status']}")
+            if k > 0:
+                lat.extend(job_ms.tolist())
+                ms.append(st["kernel_ms"])
+                rays += st["closest"] + st["shadow"]
+                launches += st["launches"]
+    res.update({"value": rays / (sum(ms) / 1000.0) / 1e6, "unit": "Mrays/s", "steps": steps,
+                "ms_per_step": statistics.mean(ms), "rays_per_step": rays / steps,
+                "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+                "latency_ms_max": float(max(lat)), "gpu_launches_per_step": launches / steps})
+    if sequential:
+        # the same jobs one after another, each its own pt_render_passes
+        flush.fill_(0)
+        torch.cuda.synchronize()
+        seq_ms, seq_rays, done = 0.0, 0, []
+        for j, r in enumerate(rs):
+            r.render_passes(spp[j] * (steps + 1), spp[j])
+            st = r.stats()
+            seq_ms += st["kernel_ms"]
+            seq_rays += st["closest"] + st["shadow"]
+            done.append(seq_ms)
+        res["sequential"] = {"value": seq_rays / (seq_ms / 1000.0) / 1e6, "unit": "Mrays/s", "ms": seq_ms,
+                             "latency_ms_p50": float(np.percentile(done, 50)),
+                             "latency_ms_p99": float(np.percentile(done, 99)),
+                             "order": "job order, device time of each render summed"}
+    for r in rs:
+        r.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,6 +367,8 @@ def main():
                     help="steps of the differentiable-materials workload for adjoint/forward (0: skip)")
     ap.add_argument("--stage-steps", type=int, default=3,
                     help="extra steps timed per kernel with CUDA events (roofline of the dominant kernel)")
+    ap.add_argument("--batch-steps", type=int, default=2,
+                    help="steps of the 64-job batched workload (p50/p99 job latency, aggregate Mrays/s; 0: skip)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
     ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
     args = ap.parse_args()
@@ -403,6 +498,11 @@ def main():
     if args.adjoint_steps > 0 and rank == 0 and not args.small:
         adjoint = adjoint_bench(args.adjoint_steps, stream, flush)
 
+    batch = None
+    if args.batch_steps > 0 and rank == 0 and not args.small:
+        r.set_stream(None)
+        batch = batch_bench(args.batch_steps, flush)
+
     # end to end through the C ABI with host buffers
     import ctypes as C
     lib = capi.load_library()
@@ -475,6 +575,8 @@ def main():
             line["compare"] = other
         if adjoint:
             line["adjoint"] = adjoint
+        if batch:
+            line["batch"] = batch
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))

@@ -4,6 +4,7 @@
 // (src/core/Renderer.cpp:41-249, 619-811).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -548,6 +549,380 @@ int pt_update_transforms(pt_context* c, const float* transforms, int32_t num_ins
     CK(cudaStreamSynchronize(c->stream));
     c->version++;
     c->fwd.valid = false;
+    return PT_OK;
+}
+
+// ---------------------------------------------------------------- batches
+}  // extern "C"
+
+struct pt_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<pt_context*> jobs;
+    std::vector<int> tlas_root, light_base;
+    uint32_t flags = 0;
+    DevBuf<WideNode> nodes;
+    DevBuf<WideTri> tris;
+    DevBuf<InstRef> insts;
+    DevBuf<InstXf> xf;
+    DevBuf<int32_t> vidx;
+    DevBuf<float4> verts, norms, mats, lights;
+    DevBuf<BatchJob> job_table;
+    DevBuf<int> remaining;
+    DevBuf<unsigned long long> done;
+    DevBuf<unsigned long long> counters;
+    DevBuf<int> status;
+    WavefrontBuffers wf;
+    WavefrontTuning tuning;
+    long chunk_paths = 1L << 25;  // paths per chunk (about 9.5 GB of path state)
+    bool use_graph = true;
+    cudaGraphExec_t graph_exec = nullptr;
+    int last_chunks = 0;
+    pt_stats last{};
+};
+
+namespace {
+__global__ void k_fix_nodes(WideNode* n, int count, int node_off, int tri_off, int inst_off, int tlas_first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    n[i].w[4] += node_off;
+    n[i].w[5] += i >= tlas_first ? inst_off : tri_off;
+}
+__global__ void k_fix_tris(WideTri* t, int count, int prim_off, int inst_off, int mat_off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    t[i].prim += prim_off;
+    t[i].e0[3] = __int_as_float(__float_as_int(t[i].e0[3]) + inst_off);  // merged BLAS: instance
+    t[i].e1[3] = __int_as_float(__float_as_int(t[i].e1[3]) + mat_off);   // and material
+}
+__global__ void k_fix_insts(InstRef* r, int count, int node_off, int inst_off, int mat_off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    r[i].blas_root += node_off;
+    if (r[i].instance != 0x7fffffff) r[i].instance += inst_off;
+    if (r[i].material >= 0) r[i].material += mat_off;
+}
+__global__ void k_fix_vidx(int32_t* v, int count, int vert_off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) v[i] += vert_off;
+}
+template <class T> cudaError_t concat(DevBuf<T>& out, const std::vector<const DevBuf<T>*>& parts, cudaStream_t s) {
+    size_t n = 0;
+    for (auto* p : parts) n += p->n;
+    cudaError_t e = out.alloc(n);
+    if (e != cudaSuccess) return e;
+    size_t off = 0;
+    for (auto* p : parts) {
+        if (p->n && (e = cudaMemcpyAsync(out.p + off, p->p, p->n * sizeof(T), cudaMemcpyDeviceToDevice, s)) !=
+                        cudaSuccess)
+            return e;
+        off += p->n;
+    }
+    return cudaSuccess;
+}
+}  // namespace
+
+extern "C" {
+
+int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
+    if (!jobs || n <= 0 || !out) return set_err(PT_ERR_INVALID_ARG, "invalid batch");
+    *out = nullptr;
+    const uint32_t unsupported = F_MEDIUM | F_ALPHA_TEST | F_ENVMAP | F_TEXTURES | F_UNIFORM_LIGHT;
+    uint32_t flags = 0;
+    for (int j = 0; j < n; ++j) {
+        pt_context* c = jobs[j];
+        if (!c) return set_err(PT_ERR_INVALID_ARG, "NULL job");
+        if (c->device != jobs[0]->device) return set_err(PT_ERR_INVALID_ARG, "batch jobs must share a device");
+        const uint32_t f = option_flags(c);
+        if (f & unsupported)
+            return set_err(PT_ERR_UNSUPPORTED, "batches take surface scenes with analytic lights only (no media, "
+                                               "alpha test, environment map, texture maps or uniform light)");
+        const uint32_t g = f & ~(uint32_t)F_LIGHTS;
+        if (j == 0) flags = g;
+        else if (g != flags) return set_err(PT_ERR_UNSUPPORTED, "batch jobs must share their render options' flags");
+    }
+    pt_batch* b = new pt_batch;
+    b->jobs.assign(jobs, jobs + n);
+    b->device = jobs[0]->device;
+    b->flags = flags | F_LIGHTS;
+    int rc = PT_OK;
+    do {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { rc = cuda_err(e, "cudaStreamCreate"); break; }
+        if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
+            rc = cuda_err(e, "cudaEventCreate");
+            break;
+        }
+        std::vector<const DevBuf<WideNode>*> pn;
+        std::vector<const DevBuf<WideTri>*> pt;
+        std::vector<const DevBuf<InstRef>*> pi;
+        std::vector<const DevBuf<InstXf>*> px;
+        std::vector<const DevBuf<int32_t>*> pv;
+        std::vector<const DevBuf<float4>*> pvert, pnorm, pmat, plight;
+        for (pt_context* c : b->jobs) {
+            CK(cudaStreamSynchronize(c->stream));
+            pn.push_back(&c->nodes);
+            pt.push_back(&c->tris);
+            pi.push_back(&c->insts);
+            px.push_back(&c->xf);
+            pv.push_back(&c->vidx);
+            pvert.push_back(&c->verts);
+            pnorm.push_back(&c->norms);
+            pmat.push_back(&c->mats);
+            plight.push_back(&c->lights);
+        }
+        if ((e = concat(b->nodes, pn, b->stream)) != cudaSuccess || (e = concat(b->tris, pt, b->stream)) != cudaSuccess ||
+            (e = concat(b->insts, pi, b->stream)) != cudaSuccess || (e = concat(b->xf, px, b->stream)) != cudaSuccess ||
+            (e = concat(b->vidx, pv, b->stream)) != cudaSuccess ||
+            (e = concat(b->verts, pvert, b->stream)) != cudaSuccess ||
+            (e = concat(b->norms, pnorm, b->stream)) != cudaSuccess ||
+            (e = concat(b->mats, pmat, b->stream)) != cudaSuccess ||
+            (e = concat(b->lights, plight, b->stream)) != cudaSuccess) {
+            rc = cuda_err(e, "batch scene concatenation");
+            break;
+        }
+        int node_off = 0, tri_off = 0, inst_off = 0, wtri_off = 0, ref_off = 0, vert_off = 0, vidx_off = 0;
+        int mat_off = 0, light_off = 0;
+        const int B = 256;
+        for (pt_context* c : b->jobs) {
+            const int nn = (int)c->nodes.n, nt = (int)c->tris.n, ni = (int)c->insts.n, nv = (int)c->vidx.n;
+            if (nn) k_fix_nodes<<<(nn + B - 1) / B, B, 0, b->stream>>>(b->nodes.p + node_off, nn, node_off, wtri_off,
+                                                                      ref_off, c->bvh.tlas_first_node);
+            if (nt) k_fix_tris<<<(nt + B - 1) / B, B, 0, b->stream>>>(b->tris.p + wtri_off, nt, tri_off, inst_off,
+                                                                     mat_off);
+            if (ni) k_fix_insts<<<(ni + B - 1) / B, B, 0, b->stream>>>(b->insts.p + ref_off, ni, node_off, inst_off,
+                                                                      mat_off);
+            if (nv) k_fix_vidx<<<(nv + B - 1) / B, B, 0, b->stream>>>(b->vidx.p + vidx_off, nv, vert_off);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            b->tlas_root.push_back(c->bvh.tlas_root + node_off);
+            b->light_base.push_back(light_off);
+            node_off += nn;
+            wtri_off += nt;
+            ref_off += ni;
+            tri_off += c->num_tris;
+            inst_off += c->num_instances;
+            vert_off += c->num_vertices;
+            vidx_off += nv;
+            mat_off += c->num_materials;
+            light_off += (int)(c->lights.n / 4);  // a job without lights holds one padding record
+        }
+        if (e != cudaSuccess) { rc = cuda_err(e, "batch index fix-up"); break; }
+        if ((e = b->counters.alloc(3)) != cudaSuccess || (e = b->status.alloc(1)) != cudaSuccess ||
+            (e = b->remaining.alloc(n)) != cudaSuccess || (e = b->done.alloc(n + 1)) != cudaSuccess) {
+            rc = cuda_err(e, "batch buffers");
+            break;
+        }
+        if ((e = wavefront_default_tuning(b->tuning, 128)) != cudaSuccess) { rc = cuda_err(e, "tuning"); break; }
+        for (pt_context* c : b->jobs)  // the launch configuration of the first tuned job
+            if (c->wf_tuned) {
+                b->tuning = c->wf_tuning;
+                break;
+            }
+        if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) { rc = cuda_err(e, "batch set-up"); break; }
+    } while (0);
+    if (rc) {
+        pt_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return PT_OK;
+}
+
+int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_passes, float* job_ms) {
+    if (!b || !first_pass || !num_passes) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    const int n = (int)b->jobs.size();
+    std::vector<BatchJob> base(n);
+    std::vector<int> remaining(n);
+    std::vector<long> job_paths(n);
+    long total = 0, max_npix = 0;
+    for (int j = 0; j < n; ++j) {
+        const pt_context* c = b->jobs[j];
+        if (first_pass[j] < 0 || num_passes[j] <= 0) return set_err(PT_ERR_INVALID_ARG, "invalid pass range");
+        const pt_render_options& o = c->opts;
+        BatchJob& J = base[j];
+        J = BatchJob{};
+        J.tlas_root = b->tlas_root[j];
+        J.light_base = b->light_base[j];
+        J.num_lights = c->num_lights;
+        J.max_depth = o.max_depth;
+        J.rr_depth = o.rr_depth;
+        J.width = o.render_width;
+        J.height = o.render_height;
+        J.tile_w = o.tile_width;
+        J.tile_h = o.tile_height;
+        J.ntx = (J.width + J.tile_w - 1) / J.tile_w;
+        J.nty = (J.height + J.tile_h - 1) / J.tile_h;
+        for (int k = 0; k < 3; ++k) {
+            J.cam_pos[k] = c->cam.position[k];
+            J.cam_up[k] = c->cam.up[k];
+            J.cam_right[k] = c->cam.right[k];
+            J.cam_fwd[k] = c->cam.forward[k];
+        }
+        J.cam_fov = c->cam.fov;
+        J.cam_focal = c->cam.focal_dist;
+        J.cam_aperture = c->cam.aperture;
+        J.accum = c->accum.p;
+        J.npix = J.width * J.height;
+        J.id = j;
+        job_paths[j] = (long)J.npix * num_passes[j];
+        if (job_paths[j] >= (1L << 31)) return set_err(PT_ERR_UNSUPPORTED, "pt_batch_render: job too large");
+        remaining[j] = (int)job_paths[j];
+        total += job_paths[j];
+        max_npix = std::max(max_npix, (long)J.npix);
+    }
+    // Whole passes are packed into chunks of at most `cap` paths (each chunk
+    // one wavefront), the jobs in order of increasing work so that short
+    // jobs complete early; a job's passes stay in pass order.
+    long cap = b->chunk_paths;
+    if (const char* e = std::getenv("PT_BATCH_CAPACITY")) cap = std::max(1L, std::atol(e));
+    cap = std::min(total, std::max(cap, max_npix));
+    if (cap > (long)INT32_MAX / 2) return set_err(PT_ERR_UNSUPPORTED, "pt_batch_render: chunk too large");
+    std::vector<int> order(n);
+    for (int j = 0; j < n; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return job_paths[x] < job_paths[y]; });
+    std::vector<BatchJob> entries;
+    std::vector<BatchChunk> chunks;
+    BatchChunk cur{0, 0, 0, 0, 0};
+    for (int j : order) {
+        const BatchJob& J = base[j];
+        int k = 0;
+        while (k < num_passes[j]) {
+            const int fit = (int)std::min<long>(num_passes[j] - k, (cap - cur.paths) / J.npix);
+            if (fit <= 0) {
+                chunks.push_back(cur);
+                cur = BatchChunk{(int)entries.size(), 0, 0, 0, 0};
+                continue;
+            }
+            BatchJob E = J;
+            E.first_pass = first_pass[j] + k;
+            E.num_passes = fit;
+            E.path_base = cur.paths;
+            E.pixel_base = cur.pixels;
+            entries.push_back(E);
+            cur.entry_count++;
+            cur.paths += fit * J.npix;
+            cur.pixels += J.npix;
+            cur.max_depth = std::max(cur.max_depth, J.max_depth);
+            k += fit;
+        }
+    }
+    if (cur.entry_count) chunks.push_back(cur);
+    if (b->wf.capacity < cap) {
+        wavefront_free(b->wf);
+        CK(wavefront_alloc(b->wf, (int)cap));
+    }
+    for (pt_context* c : b->jobs) CK(cudaStreamSynchronize(c->stream));
+    CK(b->job_table.upload(entries.data(), entries.size(), b->stream));
+    CK(cudaMemcpyAsync(b->remaining.p, remaining.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemsetAsync(b->done.p, 0, sizeof(unsigned long long) * (n + 1), b->stream));
+    CK(cudaMemsetAsync(b->counters.p, 0, 3 * sizeof(unsigned long long), b->stream));
+    CK(cudaMemsetAsync(b->status.p, 0, sizeof(int), b->stream));
+    Params p{};
+    p.nodes = reinterpret_cast<const uint4*>(b->nodes.p);
+    p.tris = reinterpret_cast<const float4*>(b->tris.p);
+    p.insts = reinterpret_cast<const int4*>(b->insts.p);
+    p.xf = reinterpret_cast<const float4*>(b->xf.p);
+    p.vidx = b->vidx.p;
+    p.verts = b->verts.p;
+    p.norms = b->norms.p;
+    p.mats = b->mats.p;
+    p.lights = b->lights.p;
+    p.num_materials = (int)(b->mats.n / 8);
+    p.flags = b->flags;
+    p.mollify_amt = b->jobs[0]->opts.roughness_mollification_amt;
+    p.counters = b->counters.p;
+    p.status = b->status.p;
+    p.jobs = b->job_table.p;
+    p.num_jobs = (int)entries.size();
+    p.job_remaining = b->remaining.p;
+    p.job_done = b->done.p;
+    WavefrontTuning t = b->tuning;
+    int depth = 0;
+    for (pt_context* c : b->jobs) depth = std::max(depth, c->bvh.tlas_depth + c->bvh.blas_depth);
+    if (!trav_postpone_fits(depth)) t.min_tris = 0;
+    int launches = 0;
+    bool use_graph = b->use_graph;
+    if (const char* e = std::getenv("PT_BATCH_GRAPH")) use_graph = std::atoi(e) != 0;
+    if (use_graph) {
+        // the whole chunk sequence as one CUDA graph (updated in place when
+        // only the kernel arguments changed since the last call)
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t ce =
+            launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches);
+        const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+        if (ce != cudaSuccess || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_err(ce != cudaSuccess ? ce : ee, "batch graph capture");
+        }
+        bool updated = false;
+        if (b->graph_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(b->graph_exec, g, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(b->graph_exec);
+                b->graph_exec = nullptr;
+            }
+        }
+        cudaError_t e = cudaSuccess;
+        if (!updated) e = cudaGraphInstantiate(&b->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->graph_exec = nullptr;
+            return cuda_err(e, "cudaGraphInstantiate");
+        }
+        CK(cudaEventRecord(b->ev0, b->stream));
+        CK(cudaGraphLaunch(b->graph_exec, b->stream));
+        CK(cudaEventRecord(b->ev1, b->stream));
+    } else {
+        CK(cudaEventRecord(b->ev0, b->stream));
+        CK(launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches));
+        CK(cudaEventRecord(b->ev1, b->stream));
+    }
+    std::vector<unsigned long long> done(n + 1);
+    unsigned long long cnt[3];
+    int st = 0;
+    CK(cudaMemcpyAsync(done.data(), b->done.p, sizeof(unsigned long long) * (n + 1), cudaMemcpyDeviceToHost,
+                       b->stream));
+    CK(cudaMemcpyAsync(cnt, b->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpyAsync(&st, b->status.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last.closest_rays = cnt[0];
+    b->last.shadow_rays = cnt[1];
+    b->last.paths = cnt[2];
+    b->last.kernel_ms = ms;
+    b->last.status = st;
+    b->last.kernel_launches = launches;
+    b->last_chunks = (int)chunks.size();
+    if (job_ms)
+        for (int j = 0; j < n; ++j) job_ms[j] = done[j] >= done[n] ? (float)((done[j] - done[n]) * 1e-6) : 0.0f;
+    for (pt_context* c : b->jobs) c->fwd.valid = false;
+    if (st) return set_err(st, "pt_batch_render: kernel status " + std::to_string(st));
+    return PT_OK;
+}
+
+int pt_batch_stats(pt_batch* b, pt_stats* s) {
+    if (!b || !s) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    *s = b->last;
+    return PT_OK;
+}
+
+int pt_batch_destroy(pt_batch* b) {
+    if (!b) return PT_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    b->nodes.free(); b->tris.free(); b->insts.free(); b->xf.free(); b->vidx.free(); b->verts.free();
+    b->norms.free(); b->mats.free(); b->lights.free(); b->job_table.free(); b->remaining.free(); b->done.free();
+    b->counters.free(); b->status.free();
+    wavefront_free(b->wf);
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
     return PT_OK;
 }
 

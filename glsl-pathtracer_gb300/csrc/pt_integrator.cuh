@@ -31,6 +31,7 @@ struct PathState {
     float scatterPdf;   // scatterSample.pdf of the last bounce (MIS weights)
     bool inMedium, surfaceScatter;
     Medium medium;      // state.medium
+    int job = 0;        // job of a batch (pt_batch_render)
 };
 
 struct HitRecord {

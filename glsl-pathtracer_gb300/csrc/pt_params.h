@@ -18,6 +18,21 @@ constexpr int kStackSize = 48;
 // overflows; deeper BVHs are traversed without postponing.
 constexpr bool trav_postpone_fits(int depth) { return 2 * depth + 3 <= kStackSize; }
 
+// One job of a batch (pt_batch_render): the values the kernels take from
+// the job instead of from Params.  Jobs are ordered by path_base.
+struct BatchJob {
+    int tlas_root;
+    int light_base, num_lights;
+    int max_depth, rr_depth;
+    int width, height, tile_w, tile_h, ntx, nty;
+    float cam_pos[3], cam_up[3], cam_right[3], cam_fwd[3];
+    float cam_fov, cam_focal, cam_aperture;
+    float4* accum;
+    int path_base, npix, num_passes, first_pass;
+    int pixel_base;  // prefix of the jobs' pixel counts
+    int id;          // the job's index in the batch (completion counters)
+};
+
 struct Params {
     // acceleration structure (bvh8.h)
     const uint4* nodes;     // WideNode, 5 x uint4
@@ -55,6 +70,12 @@ struct Params {
     float4* accum;
     unsigned long long* counters;  // [0] closest-hit queries, [1] shadow queries, [2] paths
     int* status;                   // PT_OK or a PT_ERR_* code set by the kernels
+    // batches (pt_batch_render): the jobs, paths left per job and the
+    // %globaltimer at which each job's last path finished ([num_jobs]: start)
+    const BatchJob* jobs;
+    int num_jobs;
+    int* job_remaining;
+    unsigned long long* job_done;
 };
 
 // Work description of one render launch.

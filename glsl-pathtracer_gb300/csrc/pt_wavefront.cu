@@ -63,6 +63,7 @@ __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps)
     ps.inMedium = misc.z & 1;
     ps.surfaceScatter = (misc.z >> 1) & 1;
     ps.medium.type = misc.z >> 8;
+    ps.job = misc.w;
 }
 
 __device__ __forceinline__ void store_path(const WfView& B, int i, const PathState& ps) {
@@ -73,8 +74,60 @@ __device__ __forceinline__ void store_path(const WfView& B, int i, const PathSta
     B.med[i] = make_float4(ps.medium.color.x, ps.medium.color.y, ps.medium.color.z, ps.medium.anisotropy);
     B.rng[i] = make_uint4(ps.rng.x, ps.rng.y, ps.rng.z, ps.rng.w);
     B.misc[i] = make_int4(ps.depth, ps.matID,
-                          (ps.inMedium ? 1 : 0) | (ps.surfaceScatter ? 2 : 0) | (ps.medium.type << 8), 0);
+                          (ps.inMedium ? 1 : 0) | (ps.surfaceScatter ? 2 : 0) | (ps.medium.type << 8), ps.job);
 }
+
+// ------------------------------------------------------------ batches
+// A batch renders several contexts' scenes (concatenated arrays) in one
+// sequence of stage launches; each path carries its job, whose values
+// replace Params' where they differ per job.
+__device__ __forceinline__ void job_params(Params& Pj, const BatchJob& J) {
+    Pj.tlas_root = J.tlas_root;
+    Pj.lights = Pj.lights + 4 * J.light_base;
+    Pj.num_lights = J.num_lights;
+    Pj.max_depth = J.max_depth;
+    Pj.rr_depth = J.rr_depth;
+    Pj.width = J.width;
+    Pj.height = J.height;
+    Pj.tile_w = J.tile_w;
+    Pj.tile_h = J.tile_h;
+    Pj.ntx = J.ntx;
+    Pj.nty = J.nty;
+    for (int k = 0; k < 3; ++k) {
+        Pj.cam_pos[k] = J.cam_pos[k];
+        Pj.cam_up[k] = J.cam_up[k];
+        Pj.cam_right[k] = J.cam_right[k];
+        Pj.cam_fwd[k] = J.cam_fwd[k];
+    }
+    Pj.cam_fov = J.cam_fov;
+    Pj.cam_focal = J.cam_focal;
+    Pj.cam_aperture = J.cam_aperture;
+    Pj.accum = J.accum;
+    Pj.flags &= J.num_lights > 0 ? ~0u : ~(uint32_t)F_LIGHTS;
+}
+// the job of path i (jobs ordered by path_base)
+__device__ __forceinline__ int job_of_path(const Params& P, int i) {
+    int lo = 0, hi = P.num_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.jobs[mid].path_base <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint64_t global_timer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// a path of job j has finished: the last one stamps the job's completion
+__device__ __forceinline__ void job_path_done(const Params& P, int j) {
+    if (!P.jobs) return;
+    const int id = P.jobs[j].id;
+    if (atomicSub(P.job_remaining + id, 1) == 1) P.job_done[id] = global_timer();
+}
+
+__global__ void wf_batch_stamp(unsigned long long* t) { *t = global_timer(); }
 
 // Append to a queue with one atomic per warp.
 __device__ __forceinline__ void push(int* queue, int* count, int value, bool pred) {
@@ -88,15 +141,30 @@ __device__ __forceinline__ void push(int* queue, int* count, int value, bool pre
     if (pred) queue[base + __popc(mask & ((1u << lane) - 1))] = value;
 }
 
-__global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfView B, int first_pass, int npass) {
+__global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfView B, int first_pass, int npass,
+                                                   int batch_paths = 0) {
     const int npix = W.w * W.h;
-    const int n = npix * npass;
+    const int n = P.jobs ? batch_paths : npix * npass;
     uint32_t paths = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int pix = i % npix, k = i / npix;
-        const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
         PathState ps;
-        StartPath(P, px, py, FrameNumber(P, W, first_pass + k, px, py), ps);
+        if (P.jobs) {  // batch: the job's pixel and pass, its camera
+            const int j = job_of_path(P, i);
+            const BatchJob& J = P.jobs[j];
+            Params Pj = P;
+            job_params(Pj, J);
+            const int li = i - J.path_base;
+            const int pix = li % J.npix, k = li / J.npix;
+            const int px = pix % J.width, py = pix / J.width;
+            RenderWork Wj = W;
+            Wj.tile_frame = -1;
+            StartPath(Pj, px, py, FrameNumber(Pj, Wj, J.first_pass + k, px, py), ps);
+            ps.job = j;
+        } else {
+            const int pix = i % npix, k = i / npix;
+            const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+            StartPath(P, px, py, FrameNumber(P, W, first_pass + k, px, py), ps);
+        }
         store_path(B, i, ps);
         B.q[0][i] = i;
         ++paths;
@@ -170,8 +238,16 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
                 ray = B.q[in][k];
                 const float4 o = B.o[ray], d = B.d[ray];
                 const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
-                tl = LightsClosest(P, r, B.misc[ray].x, hr);
-                trav_init(s, P, r.origin, r.direction, tl);
+                const int4 misc = B.misc[ray];
+                if (P.jobs) {
+                    Params Pj = P;
+                    job_params(Pj, P.jobs[misc.w]);
+                    tl = LightsClosest(Pj, r, misc.x, hr);
+                    trav_init(s, Pj, r.origin, r.direction, tl);
+                } else {
+                    tl = LightsClosest(P, r, misc.x, hr);
+                    trav_init(s, P, r.origin, r.direction, tl);
+                }
                 tracing = true;
                 cnt.closest++;
             }
@@ -349,7 +425,13 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 A.le[i] = make_float4(h.gle.x, h.gle.y, h.gle.z, __int_as_float(deferred ? h.light : -1));
             } else {
                 NoHook nh;
-                cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, nh);
+                if (P.jobs) {
+                    Params Pj = P;
+                    job_params(Pj, P.jobs[ps.job]);
+                    cont = ShadeStep<MEDIUM, ENV, INLINE>(Pj, ps, hr, sr, stack, cnt, nh);
+                } else {
+                    cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, nh);
+                }
             }
             if (cont && ps.depth > 65536) {  // alpha pass-through loops are bounded (pt_kernels.cu)
                 flag_status(P.status, PT_ERR_TIMEOUT);
@@ -371,6 +453,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 B.sT[i] = make_float4(sr.T.x, sr.T.y, sr.T.z, 0.0f);
             } else if (!cont) {
                 B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
+                job_path_done(P, ps.job);
             }
         }
         push(B.q[in ^ 1], B.counts + (in ^ 1), i, valid && cont);
@@ -408,12 +491,21 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
                 const float4 d = which ? B.sd1[path] : B.sd0[path];
                 const Ray r{origin, v3(d.x, d.y, d.z)};
                 cnt.shadow++;
-                if (LightsAny(P, r, d.w)) {
+                bool occluded;
+                if (P.jobs) {
+                    Params Pj = P;
+                    job_params(Pj, P.jobs[B.misc[path].w]);
+                    occluded = LightsAny(Pj, r, d.w);
+                    if (!occluded) trav_init(s, Pj, r.origin, r.direction, d.w);
+                } else {
+                    occluded = LightsAny(P, r, d.w);
+                    if (!occluded) trav_init(s, P, r.origin, r.direction, d.w);
+                }
+                if (occluded) {
                     if (which) occ1 = true;
                     else occ0 = true;
                     stage += 2;
                 } else {
-                    trav_init(s, P, r.origin, r.direction, d.w);
                     stage += 1;
                 }
             } else {
@@ -445,7 +537,10 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
             L.y = rad.y;
             L.z = rad.z;
             B.L[i] = L;
-            if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+            if (bits & 16) {
+                B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+                if (P.jobs) job_path_done(P, B.misc[i].w);
+            }
             if (ADJ && (sr.adds & 2) && !occ1) {  // the next-event term counts: its gradients too
                 const float4 le = A.le[i];
                 const int light = __float_as_int(le.w);
@@ -513,6 +608,30 @@ __global__ void __launch_bounds__(256) wf_resolve(Params P, RenderWork W, WfView
         float4 acc = *out;
         for (int k = 0; k < npass; ++k) {
             const float4 r = B.rad[(size_t)k * npix + pix];
+            acc.x += r.x;
+            acc.y += r.y;
+            acc.z += r.z;
+            acc.w += r.w;
+        }
+        *out = acc;
+    }
+}
+
+// Batch resolve: one thread per pixel of all jobs, each job's passes in order.
+__global__ void __launch_bounds__(256) wf_resolve_batch(Params P, WfView B, int total_pixels) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total_pixels; g += gridDim.x * blockDim.x) {
+        int lo = 0, hi = P.num_jobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (P.jobs[mid].pixel_base <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchJob& J = P.jobs[lo];
+        const int pix = g - J.pixel_base;
+        float4* out = J.accum + pix;
+        float4 acc = *out;
+        for (int k = 0; k < J.num_passes; ++k) {
+            const float4 r = B.rad[(size_t)J.path_base + (size_t)k * J.npix + pix];
             acc.x += r.x;
             acc.y += r.y;
             acc.z += r.z;
@@ -878,6 +997,42 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
         if ((e = launch_shadow<true>(p, v, t, A, smem, s)) != cudaSuccess) return e;
     }
     nl += 1 + 3 * iterations;
+    return cudaSuccess;
+}
+
+cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chunks, WavefrontBuffers& wb,
+                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp, int* launches) {
+    int dummy = 0;
+    int& nl = launches ? *launches : dummy;
+    nl = 0;
+    const WfView v = view_of(wb);
+    cudaError_t e;
+    wf_batch_stamp<<<1, 1, 0, s>>>(start_stamp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ++nl;
+    for (int c = 0; c < num_chunks; ++c) {
+        const BatchChunk& ch = chunks[c];
+        if (ch.paths <= 0) continue;
+        if (ch.paths > wb.capacity) return cudaErrorInvalidValue;
+        Params pc = p;
+        pc.jobs = p.jobs + ch.entry_begin;
+        pc.num_jobs = ch.entry_count;
+        const int gen_grid = std::min((ch.paths + 255) / 256, t.resident_blocks_256);
+        wf_generate<<<gen_grid, 256, 0, s>>>(pc, RenderWork{}, v, 0, 0, ch.paths);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        for (int it = 0; it <= ch.max_depth; ++it) {
+            const int in = it & 1;
+            if ((e = launch_extend(pc, v, in, t, s)) != cudaSuccess) return e;
+            if ((e = shade_dispatch(pc, v, in, t.shade_grid, t.shade_block, s, t.shade_variant, t.shade_grid_v)) !=
+                cudaSuccess)
+                return e;
+            if ((e = launch_shadow<false>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
+        }
+        const int res_grid = std::min((ch.pixels + 255) / 256, t.resident_blocks_256);
+        wf_resolve_batch<<<res_grid, 256, 0, s>>>(pc, v, ch.pixels);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        nl += 2 + 3 * (ch.max_depth + 1);
+    }
     return cudaSuccess;
 }
 

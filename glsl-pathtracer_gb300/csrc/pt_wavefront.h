@@ -99,6 +99,22 @@ struct AdjView {
 cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,
                            const AdjView& A, bool run_forward, cudaStream_t s, int* launches = nullptr);
 
+// A batch (pt_batch_render) runs as a sequence of chunks, each one wavefront
+// over the BatchJob entries [entry_begin, entry_begin + entry_count) of
+// p.jobs: whole passes of some jobs, their paths numbered consecutively
+// (paths), their pixels too (pixels), max_depth the largest of theirs.  A
+// job's passes may span several chunks, in pass order, so that its
+// accumulation adds the passes in the order a single render would.
+struct BatchChunk {
+    int entry_begin, entry_count;
+    int paths, pixels, max_depth;
+};
+// p.jobs: the whole entry table; p.job_remaining / p.job_done: indexed by
+// BatchJob::id.  start_stamp receives the global timer at the start.
+cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chunks, WavefrontBuffers& wb,
+                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp,
+                         int* launches = nullptr);
+
 // *launches (if given) receives the number of kernels launched; with a
 // timer, every launch is timed (and no graph is used).
 cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuffers& wb, const WavefrontTuning& t,

@@ -185,6 +185,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_set_stage_timing.argtypes = [P, C.c_int32]
     lib.pt_get_stage_stats.argtypes = [P, C.POINTER(pt_stage_stats)]
     lib.pt_get_stats.argtypes = [P, C.POINTER(pt_stats)]
+    lib.pt_batch_create.argtypes = [C.POINTER(P), C.c_int32, C.POINTER(P)]
+    lib.pt_batch_render.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _f]
+    lib.pt_batch_stats.argtypes = [P, C.POINTER(pt_stats)]
+    lib.pt_batch_destroy.argtypes = [P]
     lib.pt_last_error.argtypes = [C.c_char_p, C.c_size_t]
     for name in ("pt_create", "pt_create_gpu_bvh", "pt_update_transforms", "pt_gpu_build_ms", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
@@ -192,7 +196,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                  "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
                  "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune",
                  "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
-                 "pt_get_stage_stats", "pt_get_stats", "pt_last_error"):
+                 "pt_get_stage_stats", "pt_get_stats", "pt_batch_create", "pt_batch_render",
+                 "pt_batch_stats", "pt_batch_destroy", "pt_last_error"):
         getattr(lib, name).restype = C.c_int
     if path is None:
         _lib = lib
@@ -206,6 +211,7 @@ HEADER_SYMBOLS = [
     "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
     "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune", "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
     "pt_get_stage_stats", "pt_get_stats",
+    "pt_batch_create", "pt_batch_render", "pt_batch_stats", "pt_batch_destroy",
     "pt_last_error",
 ]
 

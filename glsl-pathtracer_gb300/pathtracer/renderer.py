@@ -189,3 +189,51 @@ class GpuRenderer:
             self.close()
         except Exception:
             pass
+
+
+class GpuBatch:
+    """Several GpuRenderer contexts rendered as one wavefront
+    (pt_batch_create / pt_batch_render).  Each renderer's accumulation
+    buffer receives what its own render_passes(first, count) would add."""
+
+    def __init__(self, renderers: list[GpuRenderer]):
+        self.lib = capi.load_library()
+        self.renderers = list(renderers)
+        arr = (C.c_void_p * len(self.renderers))(*[r.ctx.value for r in self.renderers])
+        self.handle = C.c_void_p()
+        capi.check(self.lib, self.lib.pt_batch_create(arr, len(self.renderers), C.byref(self.handle)))
+
+    def render(self, first_pass, num_passes) -> np.ndarray:
+        """first_pass / num_passes: one int per job (or one for all).
+        Returns each job's completion time (ms after the batch started)."""
+        n = len(self.renderers)
+        fp = np.broadcast_to(np.asarray(first_pass, np.int32), (n,)).copy()
+        npass = np.broadcast_to(np.asarray(num_passes, np.int32), (n,)).copy()
+        ms = np.zeros(n, np.float32)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        capi.check(self.lib, self.lib.pt_batch_render(self.handle, ip(fp), ip(npass),
+                                                      ms.ctypes.data_as(C.POINTER(C.c_float))))
+        return ms
+
+    def stats(self) -> dict:
+        s = capi.pt_stats()
+        capi.check(self.lib, self.lib.pt_batch_stats(self.handle, C.byref(s)))
+        return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
+                    status=s.status, launches=s.kernel_launches)
+
+    def close(self):
+        if self.handle:
+            self.lib.pt_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

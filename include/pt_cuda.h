@@ -180,6 +180,31 @@ int pt_update_transforms(pt_context* ctx, const float* transforms, int32_t num_i
 /* Device time of the last GPU BVH build (ms). */
 int pt_gpu_build_ms(pt_context* ctx, float* ms);
 
+/* Batched multi-scene rendering.  The reference renders one scene per
+ * Renderer (src/core/Renderer.cpp:41-87) and one frame per
+ * Renderer::Render call (Renderer.cpp:533-640); a renderer serving many
+ * small jobs would loop over contexts.  A batch renders the passes of
+ * several contexts in one wavefront: their device scenes are concatenated
+ * once by pt_batch_create (indices re-based), and pt_batch_render traces all
+ * jobs' paths through the same persistent kernels, each path carrying its
+ * job.  Each job's accumulation buffer receives exactly what
+ * pt_render_passes(job, first_pass[j], num_passes[j]) would add.
+ * Jobs share one device and their render options' feature flags, and carry
+ * surface scenes with analytic lights only (PT_ERR_UNSUPPORTED otherwise:
+ * no medium, alpha test, environment map, texture maps or uniform light).
+ * The batch launches with the tuning (pt_autotune / pt_set_tuning) of the
+ * first job that has one, else the default.  The contexts must outlive the
+ * batch; scene, material and light updates made to a context after
+ * pt_batch_create are not seen by the batch; camera and render-option
+ * changes (same flags) are. */
+typedef struct pt_batch pt_batch;
+int pt_batch_create(pt_context* const* jobs, int32_t num_jobs, pt_batch** out_batch);
+/* job_ms (optional, num_jobs floats): per job, the time from the start of
+ * the batch to the completion of that job's last path (device global timer). */
+int pt_batch_render(pt_batch* batch, const int32_t* first_pass, const int32_t* num_passes, float* job_ms);
+int pt_batch_stats(pt_batch* batch, pt_stats* stats);
+int pt_batch_destroy(pt_batch* batch);
+
 /* Replaces: Renderer::~Renderer (src/core/Renderer.cpp:89-133). */
 int pt_destroy(pt_context* ctx);
 
