@@ -418,6 +418,7 @@ def main():
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     rays = 0
     launches = 0
+    truncated = 0
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -429,6 +430,7 @@ def main():
             st = r.stats()  # synchronises; counters of this launch
             rays += st["closest"] + st["shadow"]
             launches += st["launches"]
+            truncated += st["truncated"]
             if st["status"] != 0:
                 raise RuntimeError(f"kernel status {st['status']}")
         torch.cuda.synchronize()
@@ -565,12 +567,16 @@ def main():
                        "integrator": args.integrator, "rays_per_step": rays_per_step,
                        "l2": "flushed before each timed step (512 MiB write)",
                        "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU",
-                       "tuning": tuning if tuning else "default"},
+                       "tuning": tuning if tuning else "default",
+                       "truncated_paths_per_step": truncated / args.steps},
             "gpu_launches": launches,
             "roofline": roofline,
             "e2e": e2e,
             "clocks": clk.summary(),
         }
+        if stages:
+            line["stages"] = {"ms_per_step": {k: v / stages["steps"] for k, v in stages["ms"].items()},
+                              "launches_per_step": {k: v / stages["steps"] for k, v in stages["launches"].items()}}
         if other:
             line["compare"] = other
         if adjoint:

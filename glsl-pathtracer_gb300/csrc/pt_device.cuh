@@ -55,6 +55,13 @@ __device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b
 __device__ __forceinline__ V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
 __device__ __forceinline__ V3 operator/(V3 a, V3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
 __device__ __forceinline__ V3 operator*(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+// a + b * s rounded after the product and after the sum, never fused: ray
+// origins (hit points, offsets) come out the same in every kernel and equal
+// the reference's GLSL evaluated without contraction, so surfaces that meet
+// at a shared plane are told apart the same way everywhere.
+__device__ __forceinline__ V3 madd_rn(V3 a, V3 b, float s) {
+    return {__fadd_rn(a.x, __fmul_rn(b.x, s)), __fadd_rn(a.y, __fmul_rn(b.y, s)), __fadd_rn(a.z, __fmul_rn(b.z, s))};
+}
 __device__ __forceinline__ V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
 __device__ __forceinline__ V3 operator/(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
 __device__ __forceinline__ V3 operator-(V3 a) { return {-a.x, -a.y, -a.z}; }

@@ -51,6 +51,13 @@ struct ShadowReq {
     float maxd[2];
     V3 contrib[2];      // misWeight * Li * f / pdf of ray k (env, light)
     V3 T;               // throughput the result is multiplied by
+    // deferred transmittance (VOL_MIS): contrib[k] holds Li, and the
+    // contribution is formed from Li * transmittance in the reference's
+    // operation order with these factors (ResolveTransmit)
+    V3 fac[2];          // env: f; light: misWeight * f
+    float mis[2];       // env: misWeight
+    float pdf[2];       // the light sample's pdf
+    bool suspended;     // a transmittance query is pending (replay, wf_shade)
 };
 
 struct Counters {
@@ -254,30 +261,58 @@ static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float 
 
 // pathtrace.glsl:118-156 (OPT_MEDIUM && OPT_VOL_MIS); each segment is counted
 // as a shadow query.
+// One hit of EvalTransmittance's segment loop (pathtrace.glsl:124-150):
+// 0 = the ray ends here (miss or light), 1 = continue from the new origin,
+// 2 = blocked (transmittance 0).  Draws a random number only at an
+// ALPHA_MODE_BLEND material.
+__device__ __forceinline__ int TransmitStep(const Params& P, const HitRecord& hr, Ray& r, V3& transmittance,
+                                            Rng& rng) {
+    if (!hr.hit || hr.isEmitter) return 0;
+    V3 normal, ffnormal;
+    Surface sf;
+    HitNormal(P, hr, r, normal, ffnormal, &sf);
+    Material mat;
+    float eta;
+    GetMaterial(P, hr.mat, 0, 0.0f, normal, ffnormal, sf, r, mat, eta);
+    bool alphatest = AlphaSkip(mat, rng);
+    bool refractive = (1.0f - mat.metallic) * mat.specTrans > 0.0f;
+    if (!(alphatest || refractive)) return 2;
+    if (dot(r.direction, normal) > 0.0f && mat.medium.type != MEDIUM_NONE) {
+        V3 color = mat.medium.type == MEDIUM_ABSORB ? v3(1.0f) - mat.medium.color : v3(1.0f);
+        transmittance = transmittance * vexp(-color * mat.medium.density * hr.t);
+    }
+    r.origin = madd_rn(madd_rn(r.origin, r.direction, hr.t), r.direction, PT_EPS);
+    return 1;
+}
+
 static __device__ __noinline__ V3 EvalTransmittance(const Params& P, Ray r, Rng& rng, uint2* stack, Counters& cnt) {
     V3 transmittance = v3(1.0f);
-    int matID = 0;
     for (int depth = 0; depth < P.max_depth; depth++) {
         HitRecord hr;
         TraceClosest(P, r, 0, hr, stack, cnt, true);
-        if (!hr.hit || hr.isEmitter) break;
-        V3 normal, ffnormal;
-        Surface sf;
-        HitNormal(P, hr, r, normal, ffnormal, &sf);
-        matID = hr.mat;
-        Material mat;
-        float eta;
-        GetMaterial(P, matID, 0, 0.0f, normal, ffnormal, sf, r, mat, eta);
-        bool alphatest = AlphaSkip(mat, rng);
-        bool refractive = (1.0f - mat.metallic) * mat.specTrans > 0.0f;
-        if (!(alphatest || refractive)) return v3(0.0f);
-        if (dot(r.direction, normal) > 0.0f && mat.medium.type != MEDIUM_NONE) {
-            V3 color = mat.medium.type == MEDIUM_ABSORB ? v3(1.0f) - mat.medium.color : v3(1.0f);
-            transmittance = transmittance * vexp(-color * mat.medium.density * hr.t);
-        }
-        r.origin = (r.origin + r.direction * hr.t) + r.direction * PT_EPS;
+        const int st = TransmitStep(P, hr, r, transmittance, rng);
+        if (st == 0) break;
+        if (st == 2) return v3(0.0f);
     }
     return transmittance;
+}
+
+// Ld of a deferred VOL_MIS request from the transmittances of its rays, with
+// the operations of DirectLight's VOL_MIS branches (pathtrace.glsl:174-190,
+// 240-256): Li *= transmittance, then the env term
+// misWeight * Li * f * envMapIntensity / lightPdf and the light term
+// misWeight * f * Li / pdf, env first.
+__device__ __forceinline__ V3 ResolveTransmit(const ShadowReq& sr, V3 T0, V3 T1, float env_intensity) {
+    V3 Ld = v3(0.0f);
+    if (sr.n & sr.adds & 1) {
+        const V3 Li = sr.contrib[0] * T0;
+        Ld = Ld + sr.mis[0] * Li * sr.fac[0] * env_intensity / sr.pdf[0];
+    }
+    if (sr.n & sr.adds & 2) {
+        const V3 Li = sr.contrib[1] * T1;
+        Ld = Ld + sr.fac[1] * Li / sr.pdf[1];
+    }
+    return Ld;
 }
 
 // ------------------------------------------------------------ envmap
@@ -410,7 +445,7 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
                                           Rng& rng, uint2* stack, Counters& cnt, ShadowReq& sr, Hook& hook) {
     V3 Ld = v3(0.0f);
     V3 Li = v3(0.0f);
-    const V3 scatterPos = fhp + normal * PT_EPS;
+    const V3 scatterPos = madd_rn(fhp, normal, PT_EPS);
     constexpr bool volmis = MEDIUM == 2;
     const V3 V = -r.direction;
     sr.n = 0;
@@ -420,13 +455,32 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
         float lightPdf;
         const V3 lightDir = SampleEnvMap(P, Li, lightPdf, rng);
         const Ray shadowRay{scatterPos, lightDir};
-        if (volmis) {
-            Li = Li * EvalTransmittance(P, shadowRay, rng, stack, cnt);
+        if (volmis && INLINE) {
+            V3 Tr;
+            if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
+                sr.suspended = true;
+                return Ld;
+            }
+            Li = Li * Tr;
             float sfPdf;
             const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, lightDir, sfPdf);
             if (sfPdf > 0.0f) {
                 float misWeight = PowerHeuristic(lightPdf, sfPdf);
                 if (misWeight > 0.0f) Ld = Ld + misWeight * Li * sf * P.env_intensity / lightPdf;
+            }
+        } else if (volmis) {  // transmittance deferred to the transmittance stage
+            float sfPdf;
+            const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, lightDir, sfPdf);
+            sr.n |= 1;
+            sr.dir[0] = lightDir;
+            sr.contrib[0] = Li;
+            sr.fac[0] = sf;
+            sr.pdf[0] = lightPdf;
+            sr.mis[0] = 0.0f;
+            if (sfPdf > 0.0f) {
+                float misWeight = PowerHeuristic(lightPdf, sfPdf);
+                sr.mis[0] = misWeight;
+                if (misWeight > 0.0f) sr.adds |= 1;
             }
         } else {
             float sfPdf = 0.0f;
@@ -470,13 +524,30 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
         Li = ls.emission;
         if (dot(ls.direction, ls.normal) < 0.0f) {
             const Ray shadowRay{scatterPos, ls.direction};
-            if (volmis) {
-                Li = Li * EvalTransmittance(P, shadowRay, rng, stack, cnt);
+            if (volmis && INLINE) {
+                V3 Tr;
+                if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
+                    sr.suspended = true;
+                    return Ld;
+                }
+                Li = Li * Tr;
                 float sfPdf;
                 const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, ls.direction, sfPdf);
                 float misWeight = 1.0f;
                 if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
                 if (sfPdf > 0.0f) Ld = Ld + misWeight * sf * Li / ls.pdf;
+            } else if (volmis) {  // transmittance deferred to the transmittance stage
+                float sfPdf;
+                const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, ls.direction, sfPdf);
+                float misWeight = 1.0f;
+                if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
+                sr.n |= 2;
+                sr.dir[1] = ls.direction;
+                sr.contrib[1] = Li;
+                sr.fac[1] = misWeight * sf;
+                sr.pdf[1] = ls.pdf;
+                sr.mis[1] = misWeight;
+                if (sfPdf > 0.0f) sr.adds |= 2;
             } else {
                 float sfPdf = 0.0f;
                 V3 c = v3(0.0f);
@@ -533,6 +604,13 @@ struct NoHook {
     __device__ __forceinline__ void vertex(const PathState&) {}
     __device__ __forceinline__ void nee_light(int, float, V3, V3, float, float, V3, V3, V3) {}
     __device__ __forceinline__ void sample(float, V3, V3, V3, V3, const PathState&, const ShadowReq&) {}
+    // EvalTransmittance of a VOL_MIS shadow ray, inline; false would suspend
+    // the shade step (the replay form, wf_shade)
+    __device__ __forceinline__ bool transmit(const Params& P, const Ray& r, Rng& rng, uint2* stack, Counters& cnt,
+                                             V3& T) {
+        T = EvalTransmittance(P, r, rng, stack, cnt);
+        return true;
+    }
 };
 
 // One iteration of PathTrace's loop (pathtrace.glsl:301-473) for the hit in
@@ -545,6 +623,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
                                           uint2* stack, Counters& cnt, Hook& hook) {
     const uint32_t F = P.flags;
     sr.n = 0;
+    sr.suspended = false;
     if (!hr.hit) {
         if ((F & F_BACKGROUND) && ps.depth == 0) ps.alpha = 0.0f;
         if (!((F & F_HIDE_EMITTERS) && !(ps.depth > 0))) {
@@ -561,7 +640,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
         }
         return false;
     }
-    const V3 fhp = ps.r.origin + ps.r.direction * hr.t;
+    const V3 fhp = madd_rn(ps.r.origin, ps.r.direction, hr.t);
     V3 normal = v3(0.0f), ffnormal = v3(0.0f);
     Surface sf;
     if (hr.prim >= 0) {
@@ -597,9 +676,10 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
                 mediumSampled = scatterDist < hr.t;
                 if (mediumSampled) {
                     ps.throughput = ps.throughput * ps.medium.color;
-                    ps.r.origin = ps.r.origin + ps.r.direction * scatterDist;
+                    ps.r.origin = madd_rn(ps.r.origin, ps.r.direction, scatterDist);
                     const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, ps.r.origin, normal, ffnormal, mat, eta,
                                                                    ps.medium, false, ps.rng, stack, cnt, sr, hook);
+                    if (sr.suspended) return false;
                     if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
                     else sr.T = ps.throughput;
                     float h1 = ps.rng.next();
@@ -620,6 +700,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
             hook.vertex(ps);
             const V3 Ld = DirectLight<MEDIUM, ENV, INLINE>(P, ps.r, fhp, normal, ffnormal, mat, eta, ps.medium, true,
                                                            ps.rng, stack, cnt, sr, hook);
+            if (sr.suspended) return false;
             if (INLINE || sr.n == 0) ps.radiance = AddScaled(ps.radiance, Ld, ps.throughput);
             else sr.T = ps.throughput;
             const V3 f = DisneySample(mat, eta, -ps.r.direction, ffnormal, scatterL, ps.scatterPdf, ps.rng);
@@ -631,7 +712,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
             }
         }
         ps.r.direction = scatterL;
-        ps.r.origin = fhp + ps.r.direction * PT_EPS;
+        ps.r.origin = madd_rn(fhp, ps.r.direction, PT_EPS);
         if (MEDIUM) {
             if (dot(ps.r.direction, normal) < 0.0f && mat.medium.type != MEDIUM_NONE) {
                 ps.inMedium = true;
@@ -712,6 +793,9 @@ __device__ __forceinline__ uint32_t FrameNumber(const Params& P, const RenderWor
     const int tx = px / P.tile_w, ty = py / P.tile_h;
     return (uint32_t)(2 + pass * P.ntx * P.nty + (P.nty - 1 - ty) * P.ntx + tx);
 }
+
+// A path ended at PT_MAX_PATH_ITERATIONS (pt_cuda.h).
+__device__ __forceinline__ void count_truncated(const Params& P) { atomicAdd(P.counters + 3, 1ull); }
 
 __device__ __forceinline__ void add_counters(const Params& P, uint32_t closest, uint32_t shadow, uint32_t paths) {
     const unsigned mask = __activemask();

@@ -33,11 +33,11 @@ __global__ void __launch_bounds__(128) render_kernel(Params P, RenderWork W) {
             PathState ps;
             StartPath(P, px, py, FrameNumber(P, W, pass, px, py), ps);
             // Alpha pass-through keeps the depth (pathtrace.glsl:423); the loop
-            // is bounded all the same, and a path that runs out reports
-            // PT_ERR_TIMEOUT.
+            // is bounded all the same (PT_MAX_PATH_ITERATIONS), and a path
+            // that runs out is counted (pt_stats.truncated_paths).
             for (int guard = 0;; ) {
-                if (++guard > 65536) {
-                    flag_status(P.status, PT_ERR_TIMEOUT);
+                if (++guard > PT_MAX_PATH_ITERATIONS) {
+                    count_truncated(P);
                     break;
                 }
                 HitRecord hr;

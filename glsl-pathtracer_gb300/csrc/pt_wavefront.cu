@@ -40,7 +40,42 @@ struct WfView {  // device pointers of WavefrontBuffers, by value
     float4* rad;
     int* q[2];
     int* qs;
-    int* counts;  // [0], [1] extension queues, [2] shadow queue, [4], [5] fetch counters of extend / shadow
+    int* counts;  // [0], [1] extension queues, [2] shadow queue, [4], [5] fetch counters of extend / shadow,
+                  // [6] resume queue (replay)
+    // replay of suspended shade steps (VOL_MIS with alpha materials): per
+    // path the transmittance of its queries 0 and 1 and the RNG state after
+    // each; the queue of paths to shade again
+    float4 *tr0, *tr1;
+    uint4 *trng0, *trng1;
+    int* qr;
+};
+
+// Transmittance queries a path's current shade step has had traced (replay):
+// bits 2-3 of misc.z, which store_path clears.
+__device__ __forceinline__ int replay_done(const WfView& B, int i) { return (B.misc[i].z >> 2) & 3; }
+
+// The replay hook: the transmittance queries of a shade step that were
+// already traced return their recorded transmittance and continue with the
+// RNG state they left; the next one suspends the step, keeping its ray and
+// the RNG state at that point for wf_transmit_replay.
+struct ReplayHook : NoHook {
+    const WfView* B;
+    int i, done, site = 0;
+    Ray ray;
+    uint4 rng_at;
+    __device__ __forceinline__ bool transmit(const Params&, const Ray& r, Rng& rng, uint2*, Counters&, V3& T) {
+        if (site < done) {
+            const float4 t = site ? B->tr1[i] : B->tr0[i];
+            const uint4 g = site ? B->trng1[i] : B->trng0[i];
+            T = v3(t.x, t.y, t.z);
+            rng.x = g.x; rng.y = g.y; rng.z = g.z; rng.w = g.w;
+            ++site;
+            return true;
+        }
+        ray = r;
+        rng_at = make_uint4(rng.x, rng.y, rng.z, rng.w);
+        return false;
+    }
 };
 
 __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps) {
@@ -81,6 +116,12 @@ __device__ __forceinline__ void store_path(const WfView& B, int i, const PathSta
 // A batch renders several contexts' scenes (concatenated arrays) in one
 // sequence of stage launches; each path carries its job, whose values
 // replace Params' where they differ per job.
+// VOL_MIS scenes without alpha materials: EvalTransmittance draws no random
+// numbers, so its rays go to the transmittance stage (wf_transmit)
+__host__ __device__ __forceinline__ bool transmit_deferred(uint32_t flags) {
+    return (flags & F_MEDIUM) && (flags & F_VOL_MIS) && !(flags & F_ALPHA_TEST);
+}
+
 __device__ __forceinline__ void job_params(Params& Pj, const BatchJob& J) {
     Pj.tlas_root = J.tlas_root;
     Pj.lights = Pj.lights + 4 * J.light_base;
@@ -359,6 +400,11 @@ struct AdjHook {
             G[k] -= W[k];  // applies only with the next-event term (unoccluded)
         }
     }
+    __device__ __forceinline__ bool transmit(const Params& P, const Ray& r, Rng& rng, uint2* stack, Counters& cnt,
+                                             V3& T) {
+        T = EvalTransmittance(P, r, rng, stack, cnt);
+        return true;
+    }
 };
 
 __device__ __forceinline__ float* adj_accumulator(const AdjView& A, float* sgrad) {
@@ -374,13 +420,18 @@ __device__ __forceinline__ void adj_flush(const AdjView& A, const float* sgrad) 
         if (sgrad[k] != 0.0f) atomicAdd(A.grad + k, sgrad[k]);
 }
 
-template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1>
+// REPLAY (VOL_MIS with alpha materials): transmittance queries suspend the
+// shade step instead of tracing inline; `in` + 2 shades the resume queue.
+template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1, bool REPLAY = false>
 __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
-    uint2 stack[INLINE ? kStackSize : 1];
+    uint2 stack[INLINE && !REPLAY ? kStackSize : 1];
     extern __shared__ float sgrad[];
     float* acc = nullptr;
     if (ADJ) acc = adj_accumulator(A, sgrad);
-    const int n = B.counts[in];
+    const bool resume = REPLAY && in >= 2;
+    in &= 1;
+    const int* queue = resume ? B.qr : B.q[in];
+    const int n = resume ? B.counts[6] : B.counts[in];
     Counters cnt{0, 0};
     for (int j0 = blockIdx.x * blockDim.x; j0 < n; j0 += gridDim.x * blockDim.x) {
         const int j = j0 + threadIdx.x;
@@ -388,7 +439,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
         bool cont = false, shadow = false;
         int i = 0;
         if (valid) {
-            i = B.q[in][j];
+            i = queue[j];
             PathState ps;
             load_path(B, i, ps);
             HitRecord hr;
@@ -423,6 +474,18 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                     A.v[3 * (size_t)i + 2] = make_float4(h.G[8], h.G[9], h.G[10], __int_as_float(h.mat));
                 }
                 A.le[i] = make_float4(h.gle.x, h.gle.y, h.gle.z, __int_as_float(deferred ? h.light : -1));
+            } else if constexpr (REPLAY) {
+                ReplayHook rh;
+                rh.B = &B;
+                rh.i = i;
+                rh.done = replay_done(B, i);
+                cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, rh);
+                if (sr.suspended) {  // the path is shaded again after its query is traced
+                    B.so[i] = make_float4(rh.ray.origin.x, rh.ray.origin.y, rh.ray.origin.z, 0.0f);
+                    B.sd0[i] = make_float4(rh.ray.direction.x, rh.ray.direction.y, rh.ray.direction.z, 0.0f);
+                    if (rh.done) B.trng1[i] = rh.rng_at;
+                    else B.trng0[i] = rh.rng_at;
+                }
             } else {
                 NoHook nh;
                 if (P.jobs) {
@@ -433,13 +496,29 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                     cont = ShadeStep<MEDIUM, ENV, INLINE>(P, ps, hr, sr, stack, cnt, nh);
                 }
             }
-            if (cont && ps.depth > 65536) {  // alpha pass-through loops are bounded (pt_kernels.cu)
-                flag_status(P.status, PT_ERR_TIMEOUT);
-                cont = false;
+            if (REPLAY && sr.suspended) {
+                shadow = true;  // to the transmittance queue; the path state stays as it was
+            } else {
+                store_path(B, i, ps);
+                shadow = !INLINE && sr.n != 0;
             }
-            store_path(B, i, ps);
-            shadow = !INLINE && sr.n != 0;
-            if (shadow) {
+            if (!REPLAY && shadow && MEDIUM == 2) {  // deferred transmittance (wf_transmit)
+                const int bits = sr.n | (sr.adds << 2) | (cont ? 0 : 16);
+                B.so[i] = make_float4(sr.origin.x, sr.origin.y, sr.origin.z, __int_as_float(bits));
+                // the hit record of this path is consumed: h0 / h2 carry the
+                // factors until the next extend stage
+                if (sr.n & 1) {
+                    B.sd0[i] = make_float4(sr.dir[0].x, sr.dir[0].y, sr.dir[0].z, sr.pdf[0]);
+                    B.sc0[i] = make_float4(sr.contrib[0].x, sr.contrib[0].y, sr.contrib[0].z, sr.mis[0]);
+                    B.h0[i] = make_float4(sr.fac[0].x, sr.fac[0].y, sr.fac[0].z, 0.0f);
+                }
+                if (sr.n & 2) {
+                    B.sd1[i] = make_float4(sr.dir[1].x, sr.dir[1].y, sr.dir[1].z, sr.pdf[1]);
+                    B.sc1[i] = make_float4(sr.contrib[1].x, sr.contrib[1].y, sr.contrib[1].z, sr.mis[1]);
+                    B.h2[i] = make_float4(sr.fac[1].x, sr.fac[1].y, sr.fac[1].z, 0.0f);
+                }
+                B.sT[i] = make_float4(sr.T.x, sr.T.y, sr.T.z, 0.0f);
+            } else if (!REPLAY && shadow) {
                 const int bits = sr.n | (sr.adds << 2) | (cont ? 0 : 16);
                 B.so[i] = make_float4(sr.origin.x, sr.origin.y, sr.origin.z, __int_as_float(bits));
                 if (sr.n & 1) {
@@ -451,7 +530,8 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                     B.sc1[i] = make_float4(sr.contrib[1].x, sr.contrib[1].y, sr.contrib[1].z, 0.0f);
                 }
                 B.sT[i] = make_float4(sr.T.x, sr.T.y, sr.T.z, 0.0f);
-            } else if (!cont) {
+            }
+            if (!shadow && !cont) {
                 B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
                 job_path_done(P, ps.job);
             }
@@ -600,6 +680,253 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
     if (ADJ) adj_flush(A, sgrad);
 }
 
+// TransmitStep out of line: the material evaluation runs once per segment,
+// and kept out of the traversal loop it does not take that loop's registers.
+static __device__ __noinline__ int transmit_hit(const Params& P, const HitRecord& hr, Ray& r, V3& T) {
+    Rng rng{0u, 0u, 0u, 0u};  // unused: no material draws (ALPHA_MODE_BLEND is absent)
+    return TransmitStep(P, hr, r, T, rng);
+}
+
+// Transmittance queries of the shadow queue (VOL_MIS scenes without alpha
+// materials, where EvalTransmittance draws no random numbers): per path the
+// env ray first, then the light ray, each a sequence of closest-hit segments
+// through refractive surfaces (EvalTransmittance, pathtrace.glsl:117-153),
+// persistent with the batched retire / refill of wf_shadow.  Each segment is
+// one shadow query.
+template <int MINB, bool PACKED>
+__global__ void __launch_bounds__(128, MINB) wf_transmit(Params P, WfView B, int refill, int min_tris) {
+    uint2 stack[kStackSize];
+    const int n = B.counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
+    Counters cnt{0, 0};
+    Trav s;
+    // per-thread stage: 0 start env ray, 1 tracing it, 2 start light ray,
+    // 3 tracing it, 4 both done
+    int path = -1, bits = 0, stage = 0, seg = 0;
+    bool exhausted = false;
+    V3 origin = v3(0.0f), T0 = v3(1.0f), T1 = v3(1.0f);
+    Ray r;
+    float tl = PT_INF;
+    bool light_hit = false;  // the segment's nearest analytic light is closer than tl
+    auto segment = [&]() {  // the next closest-hit segment of the current ray
+        cnt.shadow++;
+        HitRecord hl;
+        tl = LightsClosest(P, r, 0, hl);
+        light_hit = hl.isEmitter;
+        trav_init(s, P, r.origin, r.direction, tl);
+    };
+    auto start = [&]() {
+        if (path >= 0 && (stage == 0 || stage == 2)) {
+            const int which = stage >> 1;
+            if (bits & (1 << which)) {
+                const float4 d = which ? B.sd1[path] : B.sd0[path];
+                r = Ray{origin, v3(d.x, d.y, d.z)};
+                seg = 0;
+                if (P.max_depth > 0) {
+                    segment();
+                    stage += 1;
+                } else {
+                    stage += 2;
+                }
+            } else {
+                stage += 2;
+            }
+        }
+    };
+    auto resolve = [&]() {
+        if (path >= 0 && stage == 4) {
+            ShadowReq sr;
+            sr.n = bits & 3;
+            sr.adds = (bits >> 2) & 3;
+            if (sr.n & 1) {
+                const float4 c = B.sc0[path], d = B.sd0[path], f = B.h0[path];
+                sr.contrib[0] = v3(c.x, c.y, c.z);
+                sr.mis[0] = c.w;
+                sr.pdf[0] = d.w;
+                sr.fac[0] = v3(f.x, f.y, f.z);
+            }
+            if (sr.n & 2) {
+                const float4 c = B.sc1[path], d = B.sd1[path], f = B.h2[path];
+                sr.contrib[1] = v3(c.x, c.y, c.z);
+                sr.mis[1] = c.w;
+                sr.pdf[1] = d.w;
+                sr.fac[1] = v3(f.x, f.y, f.z);
+            }
+            const int i = path;
+            path = -1;
+            const float4 T = B.sT[i];
+            const V3 Ld = ResolveTransmit(sr, T0, T1, P.env_intensity);
+            float4 L = B.L[i];
+            const V3 rad = AddScaled(v3(L.x, L.y, L.z), Ld, v3(T.x, T.y, T.z));
+            L.x = rad.x;
+            L.y = rad.y;
+            L.z = rad.z;
+            B.L[i] = L;
+            if (bits & 16) B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
+        }
+    };
+    for (;;) {
+        start();
+        resolve();
+        if (!exhausted) {
+            const int k = fetch_work(B.counts + 5, n, path < 0);
+            exhausted = __any_sync(0xffffffffu, path < 0 && k < 0);
+            if (k >= 0) {
+                path = B.qs[k];
+                const float4 so = B.so[path];
+                bits = __float_as_int(so.w);
+                origin = v3(so.x, so.y, so.z);
+                T0 = T1 = v3(1.0f);
+                stage = 0;
+                start();
+                start();
+                resolve();
+            }
+        }
+        const bool tracing = path >= 0 && (stage == 1 || stage == 3);
+        if (!__any_sync(0xffffffffu, path >= 0)) break;
+        const int target = refill_target(exhausted, refill);
+        bool busy = tracing;
+        while (__popc(__ballot_sync(0xffffffffu, !busy)) < target) {
+            const int mode = min_tris > 0 ? trav_warp_mode(s, busy, min_tris) : TRAV_LANE;
+            if (busy && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING) {
+                HitRecord hr;
+                hr.isEmitter = light_hit;
+                FinishClosest(s, tl, hr);
+                V3 T = stage == 1 ? T0 : T1;
+                const int st = transmit_hit(P, hr, r, T);
+                if (st == 2) T = v3(0.0f);
+                if (stage == 1) T0 = T;
+                else T1 = T;
+                if (st == 1 && ++seg < P.max_depth) {
+                    segment();  // through a refractive surface: the next segment
+                } else {
+                    stage += 1;
+                    busy = false;
+                }
+            }
+        }
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
+// Paths still running after the wavefront rounds (alpha pass-through keeps
+// the depth, pathtrace.glsl:423, so a path can cross blended surfaces any
+// number of times): each thread finishes one such path as the megakernel
+// does (inline traversal, shadow rays and transmittance), bounded like the
+// megakernel's loop at PT_MAX_PATH_ITERATIONS per path in all (`rounds`
+// done in the wavefront rounds).
+template <int MEDIUM, bool ENV>
+__global__ void __launch_bounds__(128) wf_tail(Params P, WfView B, int in, int rounds) {
+    uint2 stack[kStackSize];
+    const int n = B.counts[in];
+    Counters cnt{0, 0};
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = B.q[in][j];
+        PathState ps;
+        load_path(B, i, ps);
+        for (int guard = rounds;;) {
+            if (++guard > PT_MAX_PATH_ITERATIONS) {
+                count_truncated(P);
+                break;
+            }
+            HitRecord hr;
+            TraceClosest(P, ps.r, ps.depth, hr, stack, cnt, false);
+            ShadowReq sr;
+            NoHook nh;
+            if (!ShadeStep<MEDIUM, ENV, true>(P, ps, hr, sr, stack, cnt, nh)) break;
+        }
+        B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
+// TransmitStep out of line with the path's RNG (replay: blended materials
+// draw from it).
+static __device__ __noinline__ int transmit_hit_rng(const Params& P, const HitRecord& hr, Ray& r, V3& T, Rng& rng) {
+    return TransmitStep(P, hr, r, T, rng);
+}
+
+// The suspended transmittance queries of the shadow queue (replay form):
+// EvalTransmittance's segment loop (pathtrace.glsl:117-153) from the RNG
+// state the shade step had at the query, persistent with the batched
+// retire / refill of wf_shadow; each finished query records its
+// transmittance and the RNG state after it, and queues its path to be
+// shaded again.  Each segment is one shadow query.
+template <int MINB, bool PACKED>
+__global__ void __launch_bounds__(128, MINB) wf_transmit_replay(Params P, WfView B, int refill, int min_tris) {
+    uint2 stack[kStackSize];
+    const int n = B.counts[2];
+    Counters cnt{0, 0};
+    Trav s;
+    int path = -1, seg = 0, slot = 0;
+    bool exhausted = false, tracing = false;
+    V3 T = v3(1.0f);
+    Ray r;
+    Rng rng{0u, 0u, 0u, 0u};
+    float tl = PT_INF;
+    bool light_hit = false;
+    auto segment = [&]() {
+        cnt.shadow++;
+        HitRecord hl;
+        tl = LightsClosest(P, r, 0, hl);
+        light_hit = hl.isEmitter;
+        trav_init(s, P, r.origin, r.direction, tl);
+    };
+    for (;;) {
+        // retire: record the finished queries, queue their paths again
+        const bool fin = path >= 0 && !tracing;
+        if (fin) {
+            const float4 t4 = make_float4(T.x, T.y, T.z, 0.0f);
+            const uint4 g = make_uint4(rng.x, rng.y, rng.z, rng.w);
+            if (slot) {
+                B.tr1[path] = t4;
+                B.trng1[path] = g;
+            } else {
+                B.tr0[path] = t4;
+                B.trng0[path] = g;
+            }
+            int4 m = B.misc[path];
+            m.z += 4;  // one more query traced (replay_done)
+            B.misc[path] = m;
+        }
+        push(B.qr, B.counts + 6, path, fin);
+        if (fin) path = -1;
+        if (!exhausted) {
+            const int k = fetch_work(B.counts + 5, n, path < 0);
+            exhausted = __any_sync(0xffffffffu, path < 0 && k < 0);
+            if (k >= 0) {
+                path = B.qs[k];
+                const float4 o = B.so[path], d = B.sd0[path];
+                r = Ray{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
+                slot = replay_done(B, path);
+                const uint4 g = slot ? B.trng1[path] : B.trng0[path];
+                rng.x = g.x; rng.y = g.y; rng.z = g.z; rng.w = g.w;
+                T = v3(1.0f);
+                seg = 0;
+                tracing = P.max_depth > 0;
+                if (tracing) segment();
+            }
+        }
+        if (!__any_sync(0xffffffffu, path >= 0)) break;
+        if (!__any_sync(0xffffffffu, tracing)) continue;
+        const int target = refill_target(exhausted, refill);
+        do {
+            const int mode = min_tris > 0 ? trav_warp_mode(s, tracing, min_tris) : TRAV_LANE;
+            if (tracing && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING) {
+                HitRecord hr;
+                hr.isEmitter = light_hit;
+                FinishClosest(s, tl, hr);
+                const int st = transmit_hit_rng(P, hr, r, T, rng);
+                if (st == 2) T = v3(0.0f);
+                if (st == 1 && ++seg < P.max_depth) segment();
+                else tracing = false;
+            }
+        } while (__popc(__ballot_sync(0xffffffffu, !tracing)) < target);
+    }
+    add_counters(P, cnt.closest, cnt.shadow, 0);
+}
+
 __global__ void __launch_bounds__(256) wf_resolve(Params P, RenderWork W, WfView B, int npass) {
     const int npix = W.w * W.h;
     for (int pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
@@ -650,12 +977,34 @@ WfView view_of(const WavefrontBuffers& wb) {
     v.rad = wb.rad;
     v.q[0] = wb.q[0]; v.q[1] = wb.q[1]; v.qs = wb.qs;
     v.counts = wb.counts;
+    v.tr0 = wb.tr0; v.tr1 = wb.tr1; v.trng0 = wb.trng0; v.trng1 = wb.trng1; v.qr = wb.qr;
     return v;
 }
 
 template <int MEDIUM, bool ENV, bool INLINE>
 cudaError_t launch_shade(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
     wf_shade<MEDIUM, ENV, INLINE><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_tail(const Params& p, const WfView& v, int in, int rounds, int grid, cudaStream_t s) {
+    const int medium = (p.flags & F_MEDIUM) ? ((p.flags & F_VOL_MIS) ? 2 : 1) : 0;
+    const bool env = (p.flags & F_ENVMAP) != 0;
+    switch (medium * 2 + (env ? 1 : 0)) {
+        case 0: wf_tail<0, false><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 1: wf_tail<0, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 2: wf_tail<1, false><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 3: wf_tail<1, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 4: wf_tail<2, false><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        default: wf_tail<2, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+    }
+    return cudaGetLastError();
+}
+
+// The replay form (VOL_MIS with alpha materials): in + 2 shades the resume queue.
+cudaError_t launch_shade_replay(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
+    if (p.flags & F_ENVMAP) wf_shade<2, true, true, false, 1, true><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
+    else wf_shade<2, false, true, false, 1, true><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
     return cudaGetLastError();
 }
 
@@ -676,9 +1025,10 @@ cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, i
     const int medium = (p.flags & F_MEDIUM) ? ((p.flags & F_VOL_MIS) ? 2 : 1) : 0;
     const bool env = (p.flags & F_ENVMAP) != 0;
     // AnyHit draws random numbers for alpha-tested materials without media
-    // (anyhit.glsl:118-141) and transmittance does with VOL_MIS: those keep
-    // the shadow rays inline so every path draws the reference's sequence
-    const bool inl = medium == 2 || ((p.flags & F_ALPHA_TEST) && medium == 0);
+    // (anyhit.glsl:118-141), and EvalTransmittance (VOL_MIS) at blended
+    // materials: those keep the shadow rays inline so every path draws the
+    // reference's sequence
+    const bool inl = (p.flags & F_ALPHA_TEST) && medium != 1;
     switch ((medium * 2 + (env ? 1 : 0)) * 2 + (inl ? 1 : 0)) {
         case 0: {
             const int g3[3] = {grid, grids ? grids[1] : grid, grids ? grids[2] : grid};
@@ -691,7 +1041,9 @@ cudaError_t shade_dispatch(const Params& p, const WfView& v, int in, int grid, i
         case 5: return launch_shade<1, false, true>(p, v, in, grid, block, s);
         case 6: return launch_shade<1, true, false>(p, v, in, grid, block, s);
         case 7: return launch_shade<1, true, true>(p, v, in, grid, block, s);
+        case 8: return launch_shade<2, false, false>(p, v, in, grid, block, s);
         case 9: return launch_shade<2, false, true>(p, v, in, grid, block, s);
+        case 10: return launch_shade<2, true, false>(p, v, in, grid, block, s);
         default: return launch_shade<2, true, true>(p, v, in, grid, block, s);
     }
 }
@@ -724,23 +1076,53 @@ cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity) {
     return cudaSuccess;
 }
 
+bool wavefront_needs_replay(uint32_t flags) {
+    return (flags & F_MEDIUM) && (flags & F_VOL_MIS) && (flags & F_ALPHA_TEST);
+}
+
+cudaError_t wavefront_alloc_replay(WavefrontBuffers& wb) {
+    if (wb.tr0 || wb.fixed) return cudaSuccess;
+    const size_t n = (size_t)wb.capacity;
+    cudaError_t e;
+    if ((e = cudaMalloc((void**)&wb.tr0, n * sizeof(float4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.tr1, n * sizeof(float4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.trng0, n * sizeof(uint4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.trng1, n * sizeof(uint4))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&wb.qr, n * sizeof(int))) != cudaSuccess) {
+        void* ptrs[] = {wb.tr0, wb.tr1, wb.trng0, wb.trng1, wb.qr};
+        for (void* p : ptrs)
+            if (p) cudaFree(p);
+        wb.tr0 = wb.tr1 = nullptr;
+        wb.trng0 = wb.trng1 = nullptr;
+        wb.qr = nullptr;
+        return e;
+    }
+    return cudaSuccess;
+}
+
 void wavefront_free(WavefrontBuffers& wb) {
+    if (wb.fixed) {  // the static scratch is not freed
+        if (wb.graph_exec) cudaGraphExecDestroy(wb.graph_exec);
+        wb = WavefrontBuffers{};
+        return;
+    }
     void* ptrs[] = {wb.o, wb.d, wb.T, wb.L, wb.med, wb.h0, wb.h2, wb.so, wb.sd0, wb.sd1, wb.sc0, wb.sc1, wb.sT,
-                    wb.rad, wb.rng, wb.misc, wb.h1, wb.q[0], wb.q[1], wb.qs, wb.counts};
+                    wb.rad, wb.rng, wb.misc, wb.h1, wb.q[0], wb.q[1], wb.qs, wb.counts,
+                    wb.tr0, wb.tr1, wb.trng0, wb.trng1, wb.qr};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (wb.graph_exec) cudaGraphExecDestroy(wb.graph_exec);
     wb = WavefrontBuffers{};
 }
 
-// Fixed scratch: 17 float4-sized arrays and 3 int arrays of
+// Fixed scratch: 21 float4-sized arrays and 4 int arrays of
 // kFixedScratchPaths entries, then 8 counters, each array 256-byte aligned
-// (4.4 MiB).  Nothing in it needs to start at zero: each batch's first
+// (5.5 MiB).  Nothing in it needs to start at zero: each batch's first
 // kernel (wf_generate) writes the counters and queue entries it reads.
 namespace {
 constexpr size_t kFixedVec = (size_t)kFixedScratchPaths * 16;
 constexpr size_t kFixedInt = (size_t)kFixedScratchPaths * 4;
-constexpr size_t kFixedBytes = 17 * kFixedVec + 3 * kFixedInt + 256;
+constexpr size_t kFixedBytes = 21 * kFixedVec + 4 * kFixedInt + 256;
 static_assert(kFixedVec % 256 == 0 && kFixedInt % 256 == 0, "scratch arrays stay 256-byte aligned");
 constexpr int kFixedMaxDevices = 64;
 std::atomic<char*> g_fixed_addr[kFixedMaxDevices];
@@ -762,8 +1144,9 @@ cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb) {
     }
     wb = WavefrontBuffers{};
     wb.capacity = kFixedScratchPaths;
+    wb.fixed = true;
     float4** f4[] = {&wb.o, &wb.d, &wb.T, &wb.L, &wb.med, &wb.h0, &wb.h2, &wb.so, &wb.sd0, &wb.sd1,
-                     &wb.sc0, &wb.sc1, &wb.sT, &wb.rad};
+                     &wb.sc0, &wb.sc1, &wb.sT, &wb.rad, &wb.tr0, &wb.tr1};
     size_t off = 0;
     for (float4** q : f4) {
         *q = reinterpret_cast<float4*>(base + off);
@@ -775,7 +1158,11 @@ cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb) {
     off += kFixedVec;
     wb.h1 = reinterpret_cast<int4*>(base + off);
     off += kFixedVec;
-    int** i1[] = {&wb.q[0], &wb.q[1], &wb.qs};
+    wb.trng0 = reinterpret_cast<uint4*>(base + off);
+    off += kFixedVec;
+    wb.trng1 = reinterpret_cast<uint4*>(base + off);
+    off += kFixedVec;
+    int** i1[] = {&wb.q[0], &wb.q[1], &wb.qs, &wb.qr};
     for (int** q : i1) {
         *q = reinterpret_cast<int*>(base + off);
         off += kFixedInt;
@@ -789,6 +1176,18 @@ cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb) {
 template <int MINB, bool PACKED> static const void* extend_fn() { return (const void*)wf_extend<MINB, PACKED>; }
 template <bool ADJ, int MINB, bool PACKED> static const void* shadow_fn() {
     return (const void*)wf_shadow<ADJ, MINB, PACKED>;
+}
+
+static cudaError_t launch_transmit_replay(const Params& p, const WfView& v, const WavefrontTuning& t, cudaStream_t s) {
+    const int g = t.replay_grid_v[t.shadow_variant];
+    const int b = t.shadow_block, r = t.shadow_refill, m = t.min_tris;
+    switch (t.shadow_variant) {
+        case 1: wf_transmit_replay<8, true><<<g, b, 0, s>>>(p, v, r, m); break;
+        case 2: wf_transmit_replay<6, false><<<g, b, 0, s>>>(p, v, r, m); break;
+        case 3: wf_transmit_replay<6, true><<<g, b, 0, s>>>(p, v, r, m); break;
+        default: wf_transmit_replay<8, false><<<g, b, 0, s>>>(p, v, r, m); break;
+    }
+    return cudaGetLastError();
 }
 
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
@@ -805,8 +1204,18 @@ static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const
 template <bool ADJ>
 static cudaError_t launch_shadow(const Params& p, const WfView& v, const WavefrontTuning& t, const AdjView& A,
                                  size_t smem, cudaStream_t s) {
-    const int g = t.shadow_grid_v[t.shadow_variant];
     const int b = t.shadow_block, r = t.shadow_refill, m = t.min_tris;
+    if (!ADJ && transmit_deferred(p.flags)) {
+        const int g = t.transmit_grid_v[t.shadow_variant];
+        switch (t.shadow_variant) {
+            case 1: wf_transmit<8, true><<<g, b, 0, s>>>(p, v, r, m); break;
+            case 2: wf_transmit<6, false><<<g, b, 0, s>>>(p, v, r, m); break;
+            case 3: wf_transmit<6, true><<<g, b, 0, s>>>(p, v, r, m); break;
+            default: wf_transmit<8, false><<<g, b, 0, s>>>(p, v, r, m); break;
+        }
+        return cudaGetLastError();
+    }
+    const int g = t.shadow_grid_v[t.shadow_variant];
     switch (t.shadow_variant) {
         case 1: wf_shadow<ADJ, 8, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
         case 2: wf_shadow<ADJ, 6, false><<<g, b, smem, s>>>(p, v, r, m, A); break;
@@ -861,9 +1270,54 @@ template <class F> static cudaError_t timed(StageTimer* timer, int kind, cudaStr
 }
 
 // Enqueue one batch: passes [first_pass, first_pass + npass) of the pixels of W.
+// One bounce of a batch on queue `in`: extend, shade, then the shadow stage
+// (any-hit or deferred transmittance), or in the replay form (VOL_MIS with
+// alpha materials) per transmittance query site: trace the suspended
+// queries, shade their paths again (counters: [6] resume queue, [2]
+// transmittance queue, [4] / [5] fetch counters).  Adds its kernel launches
+// to *nl.
+constexpr int kExtraRounds = 4;
+
+static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s,
+                                  StageTimer* timer, int* nl) {
+    cudaError_t e;
+    if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, in, t, s); })) != cudaSuccess) return e;
+    if (wavefront_needs_replay(p.flags)) {
+        const int sites = std::max(1, ((p.flags & F_ENVMAP) ? 1 : 0) + ((p.flags & F_LIGHTS) ? 1 : 0));
+        if ((e = timed(timer, STAGE_SHADE, s,
+                       [&] { return launch_shade_replay(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
+            return e;
+        for (int k = 0; k < sites; ++k) {
+            if ((e = timed(timer, STAGE_SHADOW, s, [&] {
+                     cudaError_t ee = cudaMemsetAsync(v.counts + 6, 0, sizeof(int), s);
+                     return ee != cudaSuccess ? ee : launch_transmit_replay(p, v, t, s);
+                 })) != cudaSuccess)
+                return e;
+            if ((e = timed(timer, STAGE_SHADE, s, [&] {
+                     cudaError_t ee = cudaMemsetAsync(v.counts + 2, 0, 4 * sizeof(int), s);
+                     return ee != cudaSuccess ? ee : launch_shade_replay(p, v, in + 2, t.shade_grid, t.shade_block, s);
+                 })) != cudaSuccess)
+                return e;
+        }
+        *nl += 2 + 2 * sites;
+        return cudaSuccess;
+    }
+    if ((e = timed(timer, STAGE_SHADE, s,
+                   [&] {
+                       return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant,
+                                             t.shade_grid_v);
+                   })) != cudaSuccess)
+        return e;
+    if ((e = timed(timer, STAGE_SHADOW, s, [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s); })) !=
+        cudaSuccess)
+        return e;
+    *nl += 3;
+    return cudaSuccess;
+}
+
 static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const WavefrontBuffers& wb, int first_pass,
                                  int npass, int iterations, const WavefrontTuning& t, cudaStream_t s,
-                                 StageTimer* timer) {
+                                 StageTimer* timer, int* nl) {
     const WfView v = view_of(wb);
     const int n = W.w * W.h * npass;
     const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
@@ -872,19 +1326,19 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
-    for (int it = 0; it < iterations; ++it) {
-        const int in = it & 1;
-        if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, in, t, s); })) != cudaSuccess)
+    *nl += 1;
+    // max_depth+1 rounds finish every path unless alpha pass-through keeps
+    // some at the same depth: those get kExtraRounds more wavefront rounds,
+    // then the tail kernel finishes the rest
+    const bool may_linger = (p.flags & F_ALPHA_TEST) != 0;
+    const int rounds = iterations + (may_linger ? kExtraRounds : 0);
+    for (int it = 0; it < rounds; ++it)
+        if ((e = enqueue_bounce(p, v, it & 1, t, s, timer, nl)) != cudaSuccess) return e;
+    if (may_linger) {
+        if ((e = timed(timer, STAGE_SHADE, s, [&] { return launch_tail(p, v, rounds & 1, rounds, t.shade_grid, s); })) !=
+            cudaSuccess)
             return e;
-        if ((e = timed(timer, STAGE_SHADE, s,
-                       [&] {
-                           return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant,
-                                                 t.shade_grid_v);
-                       })) != cudaSuccess)
-            return e;
-        if ((e = timed(timer, STAGE_SHADOW, s,
-                       [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s); })) != cudaSuccess)
-            return e;
+        *nl += 1;
     }
     return cudaSuccess;
 }
@@ -898,10 +1352,11 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
     if (W.w <= 0 || W.h <= 0 || W.num_passes <= 0) return cudaSuccess;
     const int npix = W.w * W.h;
     const int per_batch = std::max(1, std::min(W.num_passes, wb.capacity / npix));
-    // max_depth+1 extension rounds finish every path unless alpha
-    // pass-through keeps some at the same depth; those run extra rounds.
     const int iterations = p.max_depth + 1;
-    const bool may_linger = (p.flags & F_ALPHA_TEST) != 0;
+    if (wavefront_needs_replay(p.flags)) {
+        cudaError_t e = wavefront_alloc_replay(wb);
+        if (e != cudaSuccess) return e;
+    }
     const WfView v = view_of(wb);
     for (int first = W.first_pass; first < W.first_pass + W.num_passes; first += per_batch) {
         const int npass = std::min(per_batch, W.first_pass + W.num_passes - first);
@@ -909,7 +1364,8 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
         if (use_graph) {
             cudaGraph_t g = nullptr;
             if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-            cudaError_t ce = enqueue_batch(p, W, wb, first, npass, iterations, t, s, nullptr);
+            int cl = 0;
+            cudaError_t ce = enqueue_batch(p, W, wb, first, npass, iterations, t, s, nullptr, &cl);
             e = cudaStreamEndCapture(s, &g);
             if (ce != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -936,27 +1392,9 @@ cudaError_t launch_wavefront(const Params& p, const RenderWork& W, WavefrontBuff
             }
             cudaGraphDestroy(g);
             if ((e = cudaGraphLaunch(wb.graph_exec, s)) != cudaSuccess) return e;
-        } else if ((e = enqueue_batch(p, W, wb, first, npass, iterations, t, s, timer)) != cudaSuccess) {
+            nl += cl;
+        } else if ((e = enqueue_batch(p, W, wb, first, npass, iterations, t, s, timer, &nl)) != cudaSuccess) {
             return e;
-        }
-        nl += 1 + 3 * iterations;
-        if (may_linger) {
-            // bounded host loop over the remaining alpha pass-through paths
-            for (int it = iterations, guard = 0; guard < 65536; ++it, ++guard) {
-                int count = 0;
-                if ((e = cudaMemcpyAsync(&count, wb.counts + (it & 1), sizeof(int), cudaMemcpyDeviceToHost, s)) !=
-                    cudaSuccess)
-                    return e;
-                if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-                if (count == 0) break;
-                const int in = it & 1;
-                if ((e = launch_extend(p, v, in, t, s)) != cudaSuccess) return e;
-                if ((e = shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant, t.shade_grid_v)) !=
-                    cudaSuccess)
-                    return e;
-                if ((e = launch_shadow<false>(p, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
-                nl += 3;
-            }
         }
         const int res_grid = std::min((npix + 255) / 256, t.resident_blocks_256);
         if ((e = timed(timer, STAGE_RESOLVE, s, [&] {
@@ -979,9 +1417,8 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
     const int iterations = p.max_depth + 1;
     cudaError_t e;
     if (run_forward) {
-        if ((e = enqueue_batch(p, W, wb, W.first_pass, W.num_passes, iterations, t, s, nullptr)) != cudaSuccess)
+        if ((e = enqueue_batch(p, W, wb, W.first_pass, W.num_passes, iterations, t, s, nullptr, &nl)) != cudaSuccess)
             return e;
-        nl += 1 + 3 * iterations;
     }
     const WfView v = view_of(wb);
     const int n = W.w * W.h * W.num_passes;
@@ -1051,6 +1488,17 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, shd[k], block, 0);
         t.extend_grid_v[k] = sms * std::max(1, be);
         t.shadow_grid_v[k] = sms * std::max(1, bs);
+    }
+    const void* trn[4] = {(const void*)wf_transmit<8, false>, (const void*)wf_transmit<8, true>,
+                          (const void*)wf_transmit<6, false>, (const void*)wf_transmit<6, true>};
+    const void* rpl[4] = {(const void*)wf_transmit_replay<8, false>, (const void*)wf_transmit_replay<8, true>,
+                          (const void*)wf_transmit_replay<6, false>, (const void*)wf_transmit_replay<6, true>};
+    for (int k = 0; k < 4; ++k) {
+        int bt = 0, br = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bt, trn[k], block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, rpl[k], block, 0);
+        t.transmit_grid_v[k] = sms * std::max(1, bt);
+        t.replay_grid_v[k] = sms * std::max(1, br);
     }
     b_ext = t.extend_grid_v[0] / sms;
     b_shadow = t.shadow_grid_v[0] / sms;

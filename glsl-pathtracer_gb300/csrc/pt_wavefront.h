@@ -23,6 +23,12 @@ struct WavefrontBuffers {
     int* q[2] = {nullptr, nullptr};
     int* qs = nullptr;
     int* counts = nullptr;
+    // replay of suspended shade steps (VOL_MIS scenes with alpha materials),
+    // allocated by wavefront_alloc_replay when a scene needs them
+    float4 *tr0 = nullptr, *tr1 = nullptr;
+    uint4 *trng0 = nullptr, *trng1 = nullptr;
+    int* qr = nullptr;
+    bool fixed = false;  // views the static scratch (wavefront_fixed_buffers)
     cudaGraphExec_t graph_exec = nullptr;
 };
 
@@ -43,6 +49,8 @@ struct WavefrontTuning {
     // persistent grid of each variant fills the GPU
     int extend_variant = 0, shadow_variant = 0;
     int extend_grid_v[4] = {0, 0, 0, 0}, shadow_grid_v[4] = {0, 0, 0, 0};
+    int transmit_grid_v[4] = {0, 0, 0, 0};  // wf_transmit (deferred VOL_MIS transmittance), by shadow_variant
+    int replay_grid_v[4] = {0, 0, 0, 0};    // wf_transmit_replay, by shadow_variant
     // the plain surface shade stage: 0 = no register bound, 1 = 80 registers
     // (6 blocks), 2 = 64 registers (8 blocks)
     int shade_variant = 0;
@@ -74,6 +82,10 @@ constexpr int kFixedScratchPaths = 16384;
 cudaError_t wavefront_fixed_buffers(WavefrontBuffers& wb);
 cudaError_t wavefront_alloc(WavefrontBuffers& wb, int capacity);
 void wavefront_free(WavefrontBuffers& wb);
+// The replay arrays for wb.capacity paths (no-op when present).
+cudaError_t wavefront_alloc_replay(WavefrontBuffers& wb);
+// VOL_MIS scenes with alpha materials shade in the replay form.
+bool wavefront_needs_replay(uint32_t flags);
 cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block);
 // Inputs and outputs of the adjoint (path-replay backpropagation) batch.
 // The loss gradient dLoss/dI is given per pixel of the full frame, with

@@ -117,7 +117,7 @@ class GpuRenderer:
         s = capi.pt_stats()
         self._ck(self.lib.pt_get_stats(self.ctx, C.byref(s)))
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
-                    status=s.status, launches=s.kernel_launches)
+                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths)
 
     def update_materials(self, materials: np.ndarray):
         m = np.ascontiguousarray(materials, np.float32)
@@ -219,7 +219,7 @@ class GpuBatch:
         s = capi.pt_stats()
         capi.check(self.lib, self.lib.pt_batch_stats(self.handle, C.byref(s)))
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
-                    status=s.status, launches=s.kernel_launches)
+                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths)
 
     def close(self):
         if self.handle:

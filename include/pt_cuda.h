@@ -49,6 +49,15 @@ extern "C" {
 #define PT_ERR_TIMEOUT        6  /* a bounded device wait ran out */
 #define PT_ERR_QUEUE_OVERFLOW 7  /* wavefront queue capacity exceeded */
 
+/* Iterations (closest-hit query + shading) a camera path may take.  The
+ * reference's loop (pathtrace.glsl:287-423) has no bound: alpha pass-through
+ * keeps the depth (pathtrace.glsl:423), and a ray grazing a blended surface
+ * advances by EPS per crossing, so such a path can run for tens of thousands
+ * of iterations or, on a shared plane, without end.  Every integrator here
+ * (and the oracle) ends a path after this many iterations with the radiance
+ * gathered so far; pt_stats.truncated_paths counts them. */
+#define PT_MAX_PATH_ITERATIONS 4096
+
 /* ---- scene description: the reference's flattened host arrays ---------- */
 typedef struct pt_scene_desc {
     const float*   bvh_nodes;        /* 9 floats per node */
@@ -140,6 +149,7 @@ typedef struct pt_stats {
     float    kernel_ms;              /* device time of the last render call (CUDA events) */
     int32_t  status;                 /* device status word of the last call (PT_OK or PT_ERR_*) */
     int32_t  kernel_launches;        /* kernels the last render call launched */
+    uint64_t truncated_paths;        /* paths ended at PT_MAX_PATH_ITERATIONS */
 } pt_stats;
 
 #define PT_INTEGRATOR_MEGAKERNEL 0

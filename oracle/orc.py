@@ -210,6 +210,8 @@ def variant_for(scene, options) -> str:
         (False, True, True, True, False, True): "vol",
         (True, True, True, True, True, True): "envvolmis",
         (False, True, True, False, False, True): "alpha",
+        (False, True, False, True, True, True): "volmis_opaque",
+        (True, True, False, True, True, True): "envvolmis_opaque",
     }
     if key not in table:
         raise KeyError(f"no reference shader variant built for {key}")

@@ -291,6 +291,7 @@ template <class R> struct Light { V3<R> position, emission, u, v; R radius, area
 struct Counters {
     uint64_t closest = 0, shadow = 0, nodes = 0, tris = 0, overflow = 0, tri_hits = 0;
     uint64_t nodes_any = 0, tris_any = 0;  // the part of nodes / tris done by any-hit queries
+    uint64_t truncated = 0;                // paths ended at PT_MAX_PATH_ITERATIONS
 };
 
 // ------------------------------------------------------------ textures
@@ -1244,7 +1245,14 @@ template <class R> inline V3<R> PathTrace(const Scene<R>& s, Ray<R> r, Rng& rng,
     R alpha = R(1);
     bool inMedium = false, mediumSampled = false, surfaceScatter = false;
     const Flags& f = s.f;
-    for (state.depth = 0;; state.depth++) {
+    // the reference's loop has no bound; PT_MAX_PATH_ITERATIONS (pt_cuda.h)
+    // ends a path that alpha pass-through keeps at the same depth
+    state.depth = 0;
+    for (int guard = 1;; state.depth++, guard++) {
+        if (guard > PT_MAX_PATH_ITERATIONS) {
+            cnt.truncated++;
+            break;
+        }
         bool hit = ClosestHit(s, r, state, lightSample, cnt);
         if (!hit) {
             if ((f.background || f.transparent_background) && state.depth == 0) alpha = R(0);
@@ -1346,7 +1354,9 @@ template <class R> inline V3<R> PathTraceDetached(const Scene<R>& s, const Scene
     LightSampleRec<R> lightSample;
     R scatterPdf = 0;
     const Flags& f = s.f;
-    for (state.depth = 0;; state.depth++) {
+    state.depth = 0;
+    for (int guard = 1;; state.depth++, guard++) {
+        if (guard > PT_MAX_PATH_ITERATIONS) break;
         // same geometry in both scenes: the hit is the same, the light
         // emission of an emitter hit is theta's
         bool hit = ClosestHit(e, r, state, lightSample, cnt);

@@ -187,6 +187,7 @@ def test_wavefront_equals_megakernel(ptlib, name):
         sb = r.stats()
     assert sa["status"] == 0 and sb["status"] == 0
     assert sa["paths"] == sb["paths"]
+    assert sa["truncated"] == sb["truncated"]
     assert sa["closest"] + sa["shadow"] == sb["closest"] + sb["shadow"]
     # the same paths, samples and accumulation order; the two kernels are
     # compiled separately, so the compiler's fused multiply-adds in the
