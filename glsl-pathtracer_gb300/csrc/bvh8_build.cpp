@@ -56,17 +56,34 @@ struct Box {
     }
 };
 
-// A child candidate of a wide node: a binary interior node, or a primitive
-// range [first, first+count) (triangles in a BLAS, entries of the merged
-// triangle list, or one instance in the TLAS).
+// A child of a wide node: a binary interior node, or a primitive range
+// [first, first+count) (triangles in a BLAS, entries of the merged triangle
+// list, or one instance in the TLAS), or up to three primitives listed in
+// items[] (the triangles of a small binary subtree made one leaf).
 struct Child {
     int bin = -1;        // binary interior node index (range children: -1)
     int first = 0, count = 0;
+    int nitems = 0, items[3] = {0, 0, 0};
     bool merged = false;
     int blas_root = -1, material = 0;  // TLAS leaf data
     Box box;
     bool is_range() const { return bin < 0; }
     bool is_leaf_slot() const { return bin < 0 && count <= 3; }
+    int item(int q) const { return nitems ? items[q] : first + q; }
+};
+
+// SAH cost of the wide tree, per unit of surface area: a wide-node visit
+// and a primitive test (triangle, or instance entry), relative to it.
+constexpr double kCostNode = 1.0;
+constexpr double kCostPrim = 0.3;
+
+// Dynamic-programming state of a binary node (the collapse, below).
+struct Dp {
+    double c[9];          // c[i], i = 1..8: least cost of the subtree as at most i children of a wide node
+    int8_t k[9];          // i >= 2: children given to the left subtree (0: c[i] is c[i-1])
+    int8_t k8 = 0;        // the split of the best eight-child distribution (the wide node made of n)
+    bool leaf = false;    // c[1]: the subtree is one leaf child (else one internal child)
+    int np = 0;           // primitives in the subtree
 };
 
 struct MergedTri {
@@ -92,6 +109,7 @@ struct Impl {
     std::map<int, int> blas_root_map;  // binary BLAS root -> wide node index
     bool tlas = false;
     int max_depth = 0;
+    std::vector<Dp> dp;                // per binary node, filled per root by dp_solve
 };
 
 struct BuildError {
@@ -249,7 +267,143 @@ void assign_slots(const Box& node, const std::vector<Child>& kids, int slot_of[8
     }
 }
 
-void build_node(Impl& I, const std::vector<Child>& initial, int target, int depth);
+// ---------------------------------------------------------------- collapse
+// Which binary descendants become the children of each wide node is chosen
+// by dynamic programming over the binary tree for the least SAH cost, as in
+// Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs
+// Through Compressed Wide BVHs" (HPG 2017), section 3.1.  c[i] of a node is
+// the least cost of its subtree as at most i children of the wide node above:
+//   c[1] = min(leaf: A * kCostPrim * prims        if prims <= 3 (TLAS: 1),
+//              internal: A * kCostNode + D(8))
+//   c[i] = min(c[i-1], D(i)),   D(i) = min over j of left.c[j] + right.c[i-j]
+// with A the node's surface area.  The wide node made of a binary node takes
+// the children of its best eight-way distribution.  Leaves of the binary
+// tree keep their triangles (more than three: an internal child over ranges,
+// split_range); an interior node of at most three triangles may become one
+// leaf.  A greedy expansion (largest box first) instead leaves most of the
+// nodes just above the leaves with two children.
+void dp_solve(Impl& I, int root) {
+    if ((int)I.dp.size() < (int)I.bn.size()) I.dp.resize(I.bn.size());
+    const int max_leaf = I.tlas ? 1 : 3;
+    std::vector<std::pair<int, bool>> st;  // (node, children done)
+    st.push_back({root, false});
+    while (!st.empty()) {
+        auto [n, ready] = st.back();
+        st.pop_back();
+        if (n < 0 || n >= (int)I.bn.size()) fail("child node index out of range: " + std::to_string(n));
+        const BinNode& b = I.bn[n];
+        Dp& d = I.dp[n];
+        const double A = node_box(b).area();
+        if (b.leaf != 0) {
+            int np = b.leaf < 0 ? 1 : b.r;
+            if (np < 0) fail("negative triangle count in leaf " + std::to_string(n));
+            d.np = np;
+            if (np == 0) {
+                d.c[1] = 0.0;
+                d.leaf = true;
+            } else if (np <= max_leaf) {
+                d.c[1] = A * kCostPrim * np;
+                d.leaf = true;
+            } else {  // split into ranges under an internal child
+                d.c[1] = A * kCostNode + A * kCostPrim * np;
+                d.leaf = false;
+            }
+            for (int i = 2; i <= 8; ++i) { d.c[i] = d.c[1]; d.k[i] = 0; }
+            continue;
+        }
+        if (!ready) {
+            st.push_back({n, true});
+            st.push_back({b.l, false});
+            st.push_back({b.r, false});
+            continue;
+        }
+        const Dp& L = I.dp[b.l];
+        const Dp& R = I.dp[b.r];
+        d.np = L.np + R.np;
+        double D[9];
+        int8_t K[9];
+        for (int i = 2; i <= 8; ++i) {
+            D[i] = INFINITY;
+            K[i] = 1;
+            for (int j = 1; j < i; ++j) {
+                const double v = L.c[j] + R.c[i - j];
+                if (v < D[i]) { D[i] = v; K[i] = (int8_t)j; }
+            }
+        }
+        d.k8 = K[8];
+        const double cleaf = d.np <= max_leaf ? A * kCostPrim * d.np : INFINITY;
+        const double cnode = A * kCostNode + D[8];
+        d.leaf = cleaf <= cnode;
+        d.c[1] = d.leaf ? cleaf : cnode;
+        for (int i = 2; i <= 8; ++i) {
+            if (D[i] < d.c[i - 1]) { d.c[i] = D[i]; d.k[i] = K[i]; }
+            else { d.c[i] = d.c[i - 1]; d.k[i] = 0; }
+        }
+    }
+}
+
+// The binary nodes that become the (at most i) children for subtree n.
+void dp_slots(const Impl& I, int n, int i, std::vector<int>& out) {
+    const Dp& d = I.dp[n];
+    if (d.np == 0) return;  // an empty leaf contributes nothing
+    while (i > 1 && d.k[i] == 0) --i;
+    if (i == 1) { out.push_back(n); return; }
+    const BinNode& b = I.bn[n];
+    dp_slots(I, b.l, d.k[i], out);
+    dp_slots(I, b.r, i - d.k[i], out);
+}
+
+// Primitives of the subtree of n (at most three), for a leaf child.
+void gather_items(const Impl& I, int n, Child& c) {
+    const BinNode& b = I.bn[n];
+    if (b.leaf > 0) {
+        c.merged = b.leaf == 2;
+        if (c.merged && (b.l < 0 || b.l + b.r > (int)I.merged.size())) fail("merged leaf out of range");
+        for (int q = 0; q < b.r; ++q) {
+            if (c.nitems >= 3) fail("leaf of more than three primitives");
+            c.items[c.nitems++] = b.l + q;
+        }
+        range_box(I, b.l, b.r, c.merged);  // validates the indices
+        return;
+    }
+    if (b.leaf < 0) fail("TLAS leaf reached inside a BLAS (node " + std::to_string(n) + ")");
+    gather_items(I, b.l, c);
+    gather_items(I, b.r, c);
+}
+
+// The wide-node child made of binary node n as the DP chose it.
+Child child_of_slot(const Impl& I, int n) {
+    const BinNode& b = I.bn[n];
+    if (b.leaf != 0) {
+        std::vector<Child> one;
+        children_of(I, n, one);
+        if (one.size() != 1) fail("empty leaf as a child");
+        return one[0];
+    }
+    Child c;
+    c.box = node_box(b);
+    if (I.dp[n].leaf) {
+        if (I.tlas) fail("TLAS interior node as a leaf child");
+        gather_items(I, n, c);
+        c.count = c.nitems;
+        c.first = -1;
+    } else {
+        c.bin = n;
+    }
+    return c;
+}
+
+// The children of the wide node made of interior binary node n.
+void dp_children(const Impl& I, int n, std::vector<Child>& kids) {
+    const BinNode& b = I.bn[n];
+    const int k8 = I.dp[n].k8;
+    std::vector<int> slots;
+    dp_slots(I, b.l, k8, slots);
+    dp_slots(I, b.r, 8 - k8, slots);
+    for (int s : slots) kids.push_back(child_of_slot(I, s));
+}
+
+void build_node(Impl& I, const std::vector<Child>& kids, int target, int depth);
 
 // Build the wide node at index `target` from binary node / range `root`.
 void build_from(Impl& I, const Child& root, int target, int depth) {
@@ -258,36 +412,15 @@ void build_from(Impl& I, const Child& root, int target, int depth) {
         if (root.count <= 3) kids.push_back(root);
         else split_range(I, root, kids);
     } else {
-        const BinNode& n = I.bn[root.bin];
-        children_of(I, n.l, kids);
-        children_of(I, n.r, kids);
+        dp_children(I, root.bin, kids);
     }
     build_node(I, kids, target, depth);
 }
 
-void build_node(Impl& I, const std::vector<Child>& initial, int target, int depth) {
+void build_node(Impl& I, const std::vector<Child>& kids, int target, int depth) {
     if (depth > 200) fail("BVH deeper than 200 wide levels");
     I.max_depth = std::max(I.max_depth, depth);
-    std::vector<Child> kids = initial;
-    // expand interior children (largest area first) while slots remain
-    for (;;) {
-        if (kids.size() >= 8) break;
-        int best = -1;
-        double best_area = -1;
-        for (size_t i = 0; i < kids.size(); ++i) {
-            if (kids[i].is_range()) continue;
-            double a = kids[i].box.area();
-            if (a > best_area) { best_area = a; best = (int)i; }
-        }
-        if (best < 0) break;
-        std::vector<Child> sub;
-        const BinNode& n = I.bn[kids[best].bin];
-        children_of(I, n.l, sub);
-        children_of(I, n.r, sub);
-        if (kids.size() - 1 + sub.size() > 8) break;
-        kids.erase(kids.begin() + best);
-        kids.insert(kids.end(), sub.begin(), sub.end());
-    }
+    if (kids.size() > 8) fail("more than eight children");
     if (kids.empty()) fail("empty BVH node");
     Box nb;
     nb.empty();
@@ -325,7 +458,8 @@ void build_node(Impl& I, const std::vector<Child>& initial, int target, int dept
             r.identity = c.first == kMergedInstance ? 1 : I.inst_identity[c.first];
             I.insts.push_back(r);
         } else {
-            for (int k = c.first; k < c.first + c.count; ++k) {
+            for (int q = 0; q < c.count; ++q) {
+                const int k = c.item(q);
                 const int t = tri_of(I, k, c.merged);
                 WideTri wt;
                 const int32_t* vi = &I.vidx[3 * (size_t)t];
@@ -365,7 +499,10 @@ int build_root(Impl& I, int bin_root) {
     std::vector<Child> kids;
     const BinNode& n = I.bn[bin_root];
     if (n.leaf != 0) children_of(I, bin_root, kids);
-    else { children_of(I, n.l, kids); children_of(I, n.r, kids); }
+    else {
+        dp_solve(I, bin_root);
+        dp_children(I, bin_root, kids);
+    }
     if (kids.empty()) {
         // an empty leaf: a wide node with no children never hits
         std::memset(&I.nodes[target], 0, sizeof(WideNode));

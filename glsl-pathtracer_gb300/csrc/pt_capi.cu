@@ -103,6 +103,9 @@ struct pt_context {
     WavefrontBuffers wf;
     WavefrontTuning wf_tuning;
     bool wf_tuned = false;
+    // the TLAS holds one untransformed instance: traversal starts in its BLAS
+    bool direct = false;
+    InstRef entry{};
     int launches = 0;  // kernels launched by the last render call
     bool stage_timing = false;
     StageTimer timer;
@@ -147,6 +150,12 @@ Params make_params(const pt_context* c) {
     p.insts = reinterpret_cast<const int4*>(c->insts.p);
     p.xf = reinterpret_cast<const float4*>(c->xf.p);
     p.tlas_root = c->bvh.tlas_root;
+    if (c->direct) {
+        p.tlas_root = c->entry.blas_root;
+        p.direct = 1;
+        p.entry_inst = c->entry.instance;
+        p.entry_mat = c->entry.material;
+    }
     p.vidx = c->vidx.p;
     p.verts = c->verts.p;
     p.norms = c->norms.p;
@@ -240,6 +249,8 @@ int upload_bvh(pt_context* c) {
     CK(c->nodes.upload(c->bvh.nodes, c->bvh.num_nodes, c->stream));
     CK(c->tris.upload(c->bvh.tris, c->bvh.num_tris, c->stream));
     CK(c->insts.upload(c->bvh.insts, c->bvh.num_inst_refs, c->stream));
+    c->direct = c->bvh.num_inst_refs == 1 && c->bvh.insts[0].identity;
+    if (c->direct) c->entry = c->bvh.insts[0];
     if (c->bvh.tlas_depth + c->bvh.blas_depth > kStackSize)
         return set_err(PT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" +
                                                std::to_string(c->bvh.tlas_depth + c->bvh.blas_depth) + " levels)");
@@ -311,10 +322,11 @@ int end_launch(pt_context* c) {
     return PT_OK;
 }
 
-// Paths per wavefront batch: PT_WAVEFRONT_CAPACITY (default 2^24, about
-// 4.8 GB of path state), at least one full pass of the frame.
+// Paths per wavefront batch: PT_WAVEFRONT_CAPACITY (default 2^25, about
+// 9.5 GB of path state: a 16-spp 1080p frame in one batch), at least one
+// full pass of the frame.
 int wavefront_capacity(const pt_context* c, const RenderWork& w) {
-    long cap = 1L << 24;
+    long cap = 1L << 25;
     if (const char* s = std::getenv("PT_WAVEFRONT_CAPACITY")) cap = std::max(1L, std::atol(s));
     const long npix = (long)w.w * w.h;
     const long want = std::min((long)w.num_passes * npix, std::max(cap, npix));
@@ -415,6 +427,13 @@ int gpu_rebuild(pt_context* c, const float* transforms) {
     c->bvh.num_nodes = g.num_nodes;
     c->bvh.num_tris = g.num_tris;
     c->bvh.num_inst_refs = g.num_insts;
+    c->direct = false;
+    if (g.num_insts == 1) {
+        InstRef r;
+        CK(cudaMemcpy(&r, g.insts, sizeof r, cudaMemcpyDeviceToHost));
+        c->direct = r.identity != 0;
+        c->entry = r;
+    }
     c->gpu_build_ms = ms;
     return PT_OK;
 }
@@ -561,6 +580,7 @@ struct pt_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<pt_context*> jobs;
     std::vector<int> tlas_root, light_base;
+    std::vector<BatchJob> entry;  // direct BLAS entry per job (direct, entry_inst, entry_mat)
     uint32_t flags = 0;
     DevBuf<WideNode> nodes;
     DevBuf<WideTri> tris;
@@ -696,6 +716,14 @@ int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
             if (nv) k_fix_vidx<<<(nv + B - 1) / B, B, 0, b->stream>>>(b->vidx.p + vidx_off, nv, vert_off);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             b->tlas_root.push_back(c->bvh.tlas_root + node_off);
+            BatchJob entry{};
+            if (c->direct) {  // traversal starts in the BLAS, re-based like the InstRef
+                entry.direct = 1;
+                entry.entry_inst = c->entry.instance == 0x7fffffff ? c->entry.instance : c->entry.instance + inst_off;
+                entry.entry_mat = c->entry.material >= 0 ? c->entry.material + mat_off : c->entry.material;
+                b->tlas_root.back() = c->entry.blas_root + node_off;
+            }
+            b->entry.push_back(entry);
             b->light_base.push_back(light_off);
             node_off += nn;
             wtri_off += nt;
@@ -743,6 +771,9 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         BatchJob& J = base[j];
         J = BatchJob{};
         J.tlas_root = b->tlas_root[j];
+        J.direct = b->entry[j].direct;
+        J.entry_inst = b->entry[j].entry_inst;
+        J.entry_mat = b->entry[j].entry_mat;
         J.light_base = b->light_base[j];
         J.num_lights = c->num_lights;
         J.max_depth = o.max_depth;

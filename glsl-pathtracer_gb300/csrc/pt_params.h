@@ -22,6 +22,7 @@ constexpr bool trav_postpone_fits(int depth) { return 2 * depth + 3 <= kStackSiz
 // the job instead of from Params.  Jobs are ordered by path_base.
 struct BatchJob {
     int tlas_root;
+    int direct, entry_inst, entry_mat;  // as in Params
     int light_base, num_lights;
     int max_depth, rr_depth;
     int width, height, tile_w, tile_h, ntx, nty;
@@ -40,6 +41,11 @@ struct Params {
     const int4* insts;      // InstRef
     const float4* xf;       // InstXf, 10 x float4 per instance
     int tlas_root;
+    // direct != 0: the scene is one untransformed instance, and traversal
+    // starts in its BLAS (tlas_root is then the BLAS root) as instance
+    // entry_inst with material entry_mat (-1: per triangle, the merged BLAS);
+    // the hits are those of entering it from the TLAS
+    int direct, entry_inst, entry_mat;
     // reference arrays used for shading
     const int* vidx;        // Indices, 3 x int32 per triangle
     const float4* verts;    // verticesUVX

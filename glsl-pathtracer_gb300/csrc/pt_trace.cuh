@@ -311,8 +311,8 @@ __device__ __forceinline__ void trav_init(Trav& s, const Params& P, V3 o, V3 d, 
     s.pbits = 0;
     s.next = P.tlas_root;
     s.sp = 0;
-    s.cur_inst = -1;
-    s.cur_mat = 0;
+    s.cur_inst = P.direct ? P.entry_inst : -1;
+    s.cur_mat = P.direct ? P.entry_mat : 0;
 }
 
 enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };

@@ -124,6 +124,9 @@ __host__ __device__ __forceinline__ bool transmit_deferred(uint32_t flags) {
 
 __device__ __forceinline__ void job_params(Params& Pj, const BatchJob& J) {
     Pj.tlas_root = J.tlas_root;
+    Pj.direct = J.direct;
+    Pj.entry_inst = J.entry_inst;
+    Pj.entry_mat = J.entry_mat;
     Pj.lights = Pj.lights + 4 * J.light_base;
     Pj.num_lights = J.num_lights;
     Pj.max_depth = J.max_depth;
@@ -182,14 +185,18 @@ __device__ __forceinline__ void push(int* queue, int* count, int value, bool pre
     if (pred) queue[base + __popc(mask & ((1u << lane) - 1))] = value;
 }
 
+// BATCH (this kernel and the stage kernels below): the batch form
+// (pt_batch_render), compiled apart so that the single-scene kernels carry
+// none of the per-job code.
+template <bool BATCH = false>
 __global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfView B, int first_pass, int npass,
                                                    int batch_paths = 0) {
     const int npix = W.w * W.h;
-    const int n = P.jobs ? batch_paths : npix * npass;
+    const int n = BATCH ? batch_paths : npix * npass;
     uint32_t paths = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         PathState ps;
-        if (P.jobs) {  // batch: the job's pixel and pass, its camera
+        if constexpr (BATCH) {  // the job's pixel and pass, its camera
             const int j = job_of_path(P, i);
             const BatchJob& J = P.jobs[j];
             Params Pj = P;
@@ -248,7 +255,7 @@ __device__ __forceinline__ int refill_target(bool exhausted, int refill) { retur
 // unequal the rays are.
 // Traversal is memory-latency bound: 8 blocks of 128 threads (64 registers)
 // keep 32 warps per SM in flight.
-template <int MINB, bool PACKED>
+template <int MINB, bool PACKED, bool BATCH = false>
 __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
                 const float4 o = B.o[ray], d = B.d[ray];
                 const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
                 const int4 misc = B.misc[ray];
-                if (P.jobs) {
+                if constexpr (BATCH) {
                     Params Pj = P;
                     job_params(Pj, P.jobs[misc.w]);
                     tl = LightsClosest(Pj, r, misc.x, hr);
@@ -422,7 +429,7 @@ __device__ __forceinline__ void adj_flush(const AdjView& A, const float* sgrad) 
 
 // REPLAY (VOL_MIS with alpha materials): transmittance queries suspend the
 // shade step instead of tracing inline; `in` + 2 shades the resume queue.
-template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1, bool REPLAY = false>
+template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1, bool REPLAY = false, bool BATCH = false>
 __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
     uint2 stack[INLINE && !REPLAY ? kStackSize : 1];
     extern __shared__ float sgrad[];
@@ -488,7 +495,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 }
             } else {
                 NoHook nh;
-                if (P.jobs) {
+                if constexpr (BATCH) {
                     Params Pj = P;
                     job_params(Pj, P.jobs[ps.job]);
                     cont = ShadeStep<MEDIUM, ENV, INLINE>(Pj, ps, hr, sr, stack, cnt, nh);
@@ -533,7 +540,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
             }
             if (!shadow && !cont) {
                 B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
-                job_path_done(P, ps.job);
+                if (BATCH) job_path_done(P, ps.job);
             }
         }
         push(B.q[in ^ 1], B.counts + (in ^ 1), i, valid && cont);
@@ -547,7 +554,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
 // sample first, then the light sample), persistent like wf_extend, with the
 // same batched retire / refill.  The deferred form is used only when AnyHit
 // draws no random numbers.
-template <bool ADJ, int MINB, bool PACKED>
+template <bool ADJ, int MINB, bool PACKED, bool BATCH = false>
 __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int refill, int min_tris, AdjView A) {
     uint2 stack[kStackSize];
     extern __shared__ float sgrad[];
@@ -572,7 +579,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
                 const Ray r{origin, v3(d.x, d.y, d.z)};
                 cnt.shadow++;
                 bool occluded;
-                if (P.jobs) {
+                if constexpr (BATCH) {
                     Params Pj = P;
                     job_params(Pj, P.jobs[B.misc[path].w]);
                     occluded = LightsAny(Pj, r, d.w);
@@ -619,7 +626,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
             B.L[i] = L;
             if (bits & 16) {
                 B.rad[i] = make_float4(L.x, L.y, L.z, B.o[i].w);
-                if (P.jobs) job_path_done(P, B.misc[i].w);
+                if (BATCH) job_path_done(P, B.misc[i].w);
             }
             if (ADJ && (sr.adds & 2) && !occ1) {  // the next-event term counts: its gradients too
                 const float4 le = A.le[i];
@@ -1010,12 +1017,15 @@ cudaError_t launch_shade_replay(const Params& p, const WfView& v, int in, int gr
 
 // The plain surface shade (no media, no environment map, deferred shadow
 // rays) in three register budgets: unbounded, 80 (6 blocks) and 64 (8).
+template <bool BATCH = false>
 cudaError_t launch_shade_plain(const Params& p, const WfView& v, int in, int variant, const int grids[3], int block,
                                cudaStream_t s) {
+    const RenderWork w{};
+    const AdjView a{};
     switch (variant) {
-        case 1: wf_shade<0, false, false, false, 6><<<grids[1], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
-        case 2: wf_shade<0, false, false, false, 8><<<grids[2], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
-        default: wf_shade<0, false, false><<<grids[0], block, 0, s>>>(p, v, in, RenderWork{}, AdjView{}); break;
+        case 1: wf_shade<0, false, false, false, 6, false, BATCH><<<grids[1], block, 0, s>>>(p, v, in, w, a); break;
+        case 2: wf_shade<0, false, false, false, 8, false, BATCH><<<grids[2], block, 0, s>>>(p, v, in, w, a); break;
+        default: wf_shade<0, false, false, false, 1, false, BATCH><<<grids[0], block, 0, s>>>(p, v, in, w, a); break;
     }
     return cudaGetLastError();
 }
@@ -1190,18 +1200,20 @@ static cudaError_t launch_transmit_replay(const Params& p, const WfView& v, cons
     return cudaGetLastError();
 }
 
+template <bool BATCH = false>
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
     const int g = t.extend_grid_v[t.extend_variant];
+    const int b = t.extend_block, r = t.extend_refill, m = t.min_tris;
     switch (t.extend_variant) {
-        case 1: wf_extend<8, true><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
-        case 2: wf_extend<6, false><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
-        case 3: wf_extend<6, true><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
-        default: wf_extend<8, false><<<g, t.extend_block, 0, s>>>(p, v, in, t.extend_refill, t.min_tris); break;
+        case 1: wf_extend<8, true, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
+        case 2: wf_extend<6, false, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
+        case 3: wf_extend<6, true, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
+        default: wf_extend<8, false, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
     }
     return cudaGetLastError();
 }
 
-template <bool ADJ>
+template <bool ADJ, bool BATCH = false>
 static cudaError_t launch_shadow(const Params& p, const WfView& v, const WavefrontTuning& t, const AdjView& A,
                                  size_t smem, cudaStream_t s) {
     const int b = t.shadow_block, r = t.shadow_refill, m = t.min_tris;
@@ -1217,10 +1229,10 @@ static cudaError_t launch_shadow(const Params& p, const WfView& v, const Wavefro
     }
     const int g = t.shadow_grid_v[t.shadow_variant];
     switch (t.shadow_variant) {
-        case 1: wf_shadow<ADJ, 8, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
-        case 2: wf_shadow<ADJ, 6, false><<<g, b, smem, s>>>(p, v, r, m, A); break;
-        case 3: wf_shadow<ADJ, 6, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
-        default: wf_shadow<ADJ, 8, false><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        case 1: wf_shadow<ADJ, 8, true, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        case 2: wf_shadow<ADJ, 6, false, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        case 3: wf_shadow<ADJ, 6, true, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        default: wf_shadow<ADJ, 8, false, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
     }
     return cudaGetLastError();
 }
@@ -1322,7 +1334,7 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
     const int n = W.w * W.h * npass;
     const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
     cudaError_t e = timed(timer, STAGE_GENERATE, s, [&] {
-        wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, first_pass, npass);
+        wf_generate<false><<<gen_grid, 256, 0, s>>>(p, W, v, first_pass, npass);
         return cudaGetLastError();
     });
     if (e != cudaSuccess) return e;
@@ -1424,7 +1436,7 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
     const int n = W.w * W.h * W.num_passes;
     const int gen_grid = std::min((n + 255) / 256, t.resident_blocks_256);
     const size_t smem = A.shared ? sizeof(float) * (size_t)A.grad_size : 0;
-    wf_generate<<<gen_grid, 256, 0, s>>>(p, W, v, W.first_pass, W.num_passes);
+    wf_generate<false><<<gen_grid, 256, 0, s>>>(p, W, v, W.first_pass, W.num_passes);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
         const int in = it & 1;
@@ -1455,15 +1467,16 @@ cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chun
         pc.jobs = p.jobs + ch.entry_begin;
         pc.num_jobs = ch.entry_count;
         const int gen_grid = std::min((ch.paths + 255) / 256, t.resident_blocks_256);
-        wf_generate<<<gen_grid, 256, 0, s>>>(pc, RenderWork{}, v, 0, 0, ch.paths);
+        wf_generate<true><<<gen_grid, 256, 0, s>>>(pc, RenderWork{}, v, 0, 0, ch.paths);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        // batches take surface scenes with analytic lights only: the plain shade
+        const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
         for (int it = 0; it <= ch.max_depth; ++it) {
             const int in = it & 1;
-            if ((e = launch_extend(pc, v, in, t, s)) != cudaSuccess) return e;
-            if ((e = shade_dispatch(pc, v, in, t.shade_grid, t.shade_block, s, t.shade_variant, t.shade_grid_v)) !=
-                cudaSuccess)
+            if ((e = launch_extend<true>(pc, v, in, t, s)) != cudaSuccess) return e;
+            if ((e = launch_shade_plain<true>(pc, v, in, t.shade_variant, g3, t.shade_block, s)) != cudaSuccess)
                 return e;
-            if ((e = launch_shadow<false>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
+            if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
         }
         const int res_grid = std::min((ch.pixels + 255) / 256, t.resident_blocks_256);
         wf_resolve_batch<<<res_grid, 256, 0, s>>>(pc, v, ch.pixels);
