@@ -1366,7 +1366,10 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
     w.w = c->opts.render_width;
     w.h = c->opts.render_height;
     w.first_pass = 0;
-    w.num_passes = num_passes;
+    // trial frames of at least 2^22 paths: on small images a frame of a few
+    // passes is too short to time the candidates apart
+    const long npix = (long)w.w * w.h;
+    w.num_passes = (int)std::max<long>(num_passes, ((1L << 22) + npix - 1) / std::max(npix, 1L));
     w.tile_frame = -1;
     w.tile_x = w.tile_y = 0;
     const int cap = wavefront_capacity(c, w);

@@ -439,7 +439,8 @@ static __device__ __noinline__ V3 DisneyEval(const Material& mat, float eta, V3 
 }
 
 // disney.glsl:142-242
-__device__ __forceinline__ V3 DisneySample(const Material& mat, float eta, V3 V, V3 N, V3& L, float& pdf, Rng& rng) {
+static __device__ __noinline__ V3 DisneySample(const Material& mat, float eta, V3 V, V3 N, V3& L, float& pdf,
+                                              Rng& rng) {
     pdf = 0.0f;
     float r1 = rng.next();
     float r2 = rng.next();

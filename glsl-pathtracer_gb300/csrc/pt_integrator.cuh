@@ -186,11 +186,12 @@ __device__ __forceinline__ V3 pow22(float4 t) { return v3(powf(t.x, 2.2f), powf(
 // (base colour and opacity, metallic-roughness, normal map -- which bends
 // normal / ffnormal -- and emission), roughness mollification, then ax / ay
 // and eta.
-__device__ __forceinline__ void GetMaterial(const Params& P, int matID, int depth, float prevRough, V3& normal,
-                                            V3& ffnormal, const Surface& sf, const Ray& r, Material& mat,
-                                            float& eta) {
-    LoadMaterial(P.mats, matID, mat);
-    if (P.flags & F_TEXTURES) {
+// The texture-map part of GetMaterial, out of line: scenes without texture
+// maps keep it out of the shading kernels' instruction stream.
+static __device__ __noinline__ void ApplyTextureMaps(const Params& P, int matID, int depth, float prevRough,
+                                                     V3& normal, V3& ffnormal, const Surface& sf, const Ray& r,
+                                                     Material& mat) {
+    {
         const float4 ids = __ldg(P.mats + 8 * matID + 6);  // baseColor, metallicRoughness, normalmap, emission
         if ((int)ids.x >= 0) {
             const float4 t = SampleTexArray(P, sf.u, sf.v, ids.x);
@@ -214,9 +215,16 @@ __device__ __forceinline__ void GetMaterial(const Params& P, int matID, int dept
         if ((P.flags & F_MOLLIFY) && depth > 0)
             mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
         if ((int)ids.w >= 0) mat.emission = pow22(SampleTexArray(P, sf.u, sf.v, ids.w));
-    } else if ((P.flags & F_MOLLIFY) && depth > 0) {
-        mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
     }
+}
+
+__device__ __forceinline__ void GetMaterial(const Params& P, int matID, int depth, float prevRough, V3& normal,
+                                            V3& ffnormal, const Surface& sf, const Ray& r, Material& mat,
+                                            float& eta) {
+    LoadMaterial(P.mats, matID, mat);
+    if (P.flags & F_TEXTURES) ApplyTextureMaps(P, matID, depth, prevRough, normal, ffnormal, sf, r, mat);
+    else if ((P.flags & F_MOLLIFY) && depth > 0)
+        mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
     FinishMaterial(mat);
     eta = dot(r.direction, normal) < 0.0f ? (1.0f / mat.ior) : mat.ior;
 }

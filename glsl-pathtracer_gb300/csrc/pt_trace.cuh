@@ -242,7 +242,7 @@ __device__ __forceinline__ V3 xform_point(const float4* __restrict__ xf, int ins
 
 // texture(textureMapsArrayTex, vec3(uv, layer)): bilinear, GL_REPEAT, texel
 // centres at (i + 0.5) / size, the layer rounded and clamped; RGBA8 / 255.
-__device__ __forceinline__ float4 SampleTexArray(const Params& P, float u, float v, float layerf) {
+static __device__ __noinline__ float4 SampleTexArray(const Params& P, float u, float v, float layerf) {
     int layer = (int)floorf(layerf + 0.5f);
     layer = min(max(layer, 0), P.num_tex - 1);
     const int w = P.tex_w, h = P.tex_h;
