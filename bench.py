@@ -146,9 +146,9 @@ class ClockSampler:
 
 # DRAM bytes per closest-hit query of wf_extend on the icosphere workload:
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch / its rays, from
-# profiles/wf_extend_wf_shadow_icosphere_1m_1spp.md (traffic grows with the
+# profiles/wf_extend_wf_shade_wf_shadow_icosphere_1m_1spp.md (traffic grows with the
 # rays of a launch: path-state reads and writes, BVH misses in L2).
-EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 95.3}
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 94.3}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
