@@ -1419,7 +1419,7 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
         best.extend_variant = ve;
         best.shadow_variant = vs;
         // 2. refill thresholds, separately
-        const int refills[] = {4, 8, 12, 16};
+        const int refills[] = {8, 12, 16, 20, 24, 28};
         be = bs = 1e30f;
         int re = best.extend_refill, rs = best.shadow_refill;
         for (int r : refills) {

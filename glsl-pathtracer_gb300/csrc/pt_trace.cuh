@@ -317,6 +317,12 @@ __device__ __forceinline__ void trav_init(Trav& s, const Params& P, V3 o, V3 d, 
 
 enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };
 
+// Triangles a triangle step tests: a whole leaf child (at most three).  A
+// step's fixed cost (the warp's mode vote, the loop's ballots, the branch
+// into the triangle code) is then paid once per leaf rather than once per
+// triangle.
+constexpr int kTrisPerStep = 3;
+
 __device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp, uint2 e) {
     if (sp < kStackSize) stack[sp++] = e;
     else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
@@ -357,43 +363,50 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         s.pbits = 0;
     }
     if (s.pbits) {
-        const int b = __ffs(s.pbits) - 1;
-        s.pbits &= s.pbits - 1;
         if (in_blas) {
-            if (s.pbits) prefetch_l1(P.tris + 3 * (size_t)(s.pbase + __ffs(s.pbits) - 1));
-            float u, v, t, w;
-            int prim, tinst, tmat;
-            if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim, tinst, tmat)) {
-                // the merged BLAS of untransformed instances (cur_mat < 0)
-                // carries instance and material per triangle
-                const int mat = s.cur_mat < 0 ? tmat : s.cur_mat;
-                const int inst = s.cur_mat < 0 ? tinst : s.cur_inst;
-                if (ANY) {
-                    if (t < s.tmax) {
-                        if (!ALPHA) return TRAV_HIT;
-                        const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
-                        const int alphaMode = (int)ap.y;
-                        float opacity = ap.x;
-                        if (P.flags & F_TEXTURES) {  // the base-colour map's alpha (layer 0 when none)
-                            float tu, tv;
-                            TriTexCoord(P, prim, u, v, w, tu, tv);
-                            opacity *= SampleTexArray(P, tu, tv, __ldg(P.mats + 8 * mat + 6).x).w;
+            // up to kTrisPerStep of the pending triangles (in bit order)
+#pragma unroll
+            for (int q = 0; q < kTrisPerStep; ++q) {
+                if (q > 0 && !s.pbits) break;
+                const int b = __ffs(s.pbits) - 1;
+                s.pbits &= s.pbits - 1;
+                if (s.pbits) prefetch_l1(P.tris + 3 * (size_t)(s.pbase + __ffs(s.pbits) - 1));
+                float u, v, t, w;
+                int prim, tinst, tmat;
+                if (tri_test(s.cur, P.tris, s.pbase + b, s.tmax, u, v, t, w, prim, tinst, tmat)) {
+                    // the merged BLAS of untransformed instances (cur_mat < 0)
+                    // carries instance and material per triangle
+                    const int mat = s.cur_mat < 0 ? tmat : s.cur_mat;
+                    const int inst = s.cur_mat < 0 ? tinst : s.cur_inst;
+                    if (ANY) {
+                        if (t < s.tmax) {
+                            if (!ALPHA) return TRAV_HIT;
+                            const float4 ap = __ldg(P.mats + 8 * mat + 7);  // opacity, alphaMode, cutoff
+                            const int alphaMode = (int)ap.y;
+                            float opacity = ap.x;
+                            if (P.flags & F_TEXTURES) {  // the base-colour map's alpha (layer 0 when none)
+                                float tu, tv;
+                                TriTexCoord(P, prim, u, v, w, tu, tv);
+                                opacity *= SampleTexArray(P, tu, tv, __ldg(P.mats + 8 * mat + 6).x).w;
+                            }
+                            bool skip = alphaMode == ALPHA_MODE_MASK && opacity < ap.z;
+                            if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > opacity;
+                            if (!skip) return TRAV_HIT;
                         }
-                        bool skip = alphaMode == ALPHA_MODE_MASK && opacity < ap.z;
-                        if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > opacity;
-                        if (!skip) return TRAV_HIT;
+                    } else if (t < s.tmax || (s.prim >= 0 && (prim < s.prim || (prim == s.prim && inst < s.inst)))) {
+                        s.tmax = t;
+                        s.u = u;
+                        s.v = v;
+                        s.prim = prim;
+                        s.inst = inst;
+                        s.mat = mat;
                     }
-                } else if (t < s.tmax || (s.prim >= 0 && (prim < s.prim || (prim == s.prim && inst < s.inst)))) {
-                    s.tmax = t;
-                    s.u = u;
-                    s.v = v;
-                    s.prim = prim;
-                    s.inst = inst;
-                    s.mat = mat;
                 }
             }
         } else {
             // enter an instance: park the TLAS position on the stack
+            const int b = __ffs(s.pbits) - 1;
+            s.pbits &= s.pbits - 1;
             const int4 ir = __ldg(P.insts + s.pbase + b);
             trav_push(P, stack, s.sp, s.ng);
             trav_push(P, stack, s.sp, make_uint2(s.pbase, s.pbits));

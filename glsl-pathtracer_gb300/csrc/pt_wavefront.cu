@@ -359,8 +359,11 @@ struct AdjHook {
     }
     // out[k] += sum_c w1_c df_c/dtheta_k (and the same with w2 into out2)
     template <bool TWO>
+    // All 11 partial derivatives in one forward-mode evaluation: one primal
+    // BSDF evaluation instead of one per chunk (measured fastest on GB300
+    // against chunks of 4 and 6, despite the wider duals).
     __device__ __forceinline__ void df(float eta, V3 V, V3 N, V3 L, V3 w1, V3 w2, float* out, float* out2) const {
-        constexpr int NC = 4;
+        constexpr int NC = grad::kParams;
 #pragma unroll 1
         for (int chunk = 0; chunk * NC < grad::kParams; ++chunk) {
             const grad::MatD<NC> m = grad::LoadMaterialD<NC>(P->mats, mat, chunk, mollify, mollified);

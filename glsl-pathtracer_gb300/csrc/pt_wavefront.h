@@ -37,7 +37,7 @@ struct WavefrontTuning {
     int extend_block = 128, shade_block = 128, shadow_block = 128;
     // idle lanes of a warp that trigger a retire + refill round in the
     // persistent extend / shadow kernels (PT_WAVEFRONT_REFILL overrides)
-    int extend_refill = 12, shadow_refill = 12;
+    int extend_refill = 20, shadow_refill = 20;
     // triangle steps run when at least min_tris lanes of a warp have
     // triangles pending; fewer are postponed (0: every lane steps on its own;
     // PT_WAVEFRONT_MIN_TRIS overrides).  Needs trav_postpone_fits(depth).
