@@ -78,8 +78,12 @@ struct ReplayHook : NoHook {
     }
 };
 
+// MEDIUM == 0 (no media in the scene): the medium record is never read or
+// written (its fields keep StartPath's values, which nothing reads).
+template <int MEDIUM = 1>
 __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps) {
-    const float4 o = B.o[i], d = B.d[i], T = B.T[i], L = B.L[i], m = B.med[i];
+    const float4 o = B.o[i], d = B.d[i], T = B.T[i], L = B.L[i];
+    const float4 m = MEDIUM ? B.med[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const uint4 g = B.rng[i];
     const int4 misc = B.misc[i];
     ps.r.origin = v3(o.x, o.y, o.z);
@@ -101,12 +105,13 @@ __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps)
     ps.job = misc.w;
 }
 
+template <int MEDIUM = 1>
 __device__ __forceinline__ void store_path(const WfView& B, int i, const PathState& ps) {
     B.o[i] = make_float4(ps.r.origin.x, ps.r.origin.y, ps.r.origin.z, ps.alpha);
     B.d[i] = make_float4(ps.r.direction.x, ps.r.direction.y, ps.r.direction.z, ps.scatterPdf);
     B.T[i] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.prevRough);
     B.L[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.medium.density);
-    B.med[i] = make_float4(ps.medium.color.x, ps.medium.color.y, ps.medium.color.z, ps.medium.anisotropy);
+    if (MEDIUM) B.med[i] = make_float4(ps.medium.color.x, ps.medium.color.y, ps.medium.color.z, ps.medium.anisotropy);
     B.rng[i] = make_uint4(ps.rng.x, ps.rng.y, ps.rng.z, ps.rng.w);
     B.misc[i] = make_int4(ps.depth, ps.matID,
                           (ps.inMedium ? 1 : 0) | (ps.surfaceScatter ? 2 : 0) | (ps.medium.type << 8), ps.job);
@@ -276,7 +281,8 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
             B.h0[ray] = make_float4(hr.t, hr.u, hr.v, hr.w);
             B.h1[ray] = make_int4(hr.prim, hr.inst, hr.mat,
                                   (hr.hit ? 1 : 0) | (hr.isEmitter ? 2 | (hr.light << 2) : 0));
-            B.h2[ray] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
+            if (hr.isEmitter)  // read by the shade stage for light hits only
+                B.h2[ray] = make_float4(hr.lightEmission.x, hr.lightEmission.y, hr.lightEmission.z, hr.lightPdf);
             ray = -1;
         }
         if (!exhausted) {  // refill
@@ -451,17 +457,23 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
         if (valid) {
             i = queue[j];
             PathState ps;
-            load_path(B, i, ps);
+            load_path<MEDIUM>(B, i, ps);
             HitRecord hr;
-            const float4 h0 = B.h0[i], h2 = B.h2[i];
+            const float4 h0 = B.h0[i];
             const int4 h1 = B.h1[i];
             hr.t = h0.x; hr.u = h0.y; hr.v = h0.z; hr.w = h0.w;
             hr.prim = h1.x; hr.inst = h1.y; hr.mat = h1.z;
             hr.hit = h1.w & 1;
             hr.isEmitter = (h1.w >> 1) & 1;
             hr.light = h1.w >> 2;
-            hr.lightEmission = v3(h2.x, h2.y, h2.z);
-            hr.lightPdf = h2.w;
+            if (hr.isEmitter) {  // the light's emission and pdf (written by the extend stage for light hits)
+                const float4 h2 = B.h2[i];
+                hr.lightEmission = v3(h2.x, h2.y, h2.z);
+                hr.lightPdf = h2.w;
+            } else {
+                hr.lightEmission = v3(0.0f);
+                hr.lightPdf = 0.0f;
+            }
             ShadowReq sr;
             if constexpr (ADJ) {
                 AdjHook h;
@@ -509,7 +521,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
             if (REPLAY && sr.suspended) {
                 shadow = true;  // to the transmittance queue; the path state stays as it was
             } else {
-                store_path(B, i, ps);
+                store_path<MEDIUM>(B, i, ps);
                 shadow = !INLINE && sr.n != 0;
             }
             if (!REPLAY && shadow && MEDIUM == 2) {  // deferred transmittance (wf_transmit)
