@@ -264,3 +264,19 @@ def test_wide_bvh_collapse_is_conservative_and_complete(which):
     assert info["blas_depth"] + info["tlas_depth"] <= 48
     if which == "icosphere":  # all instances untransformed: one merged BLAS
         assert len(insts) == 1 and insts[0, 1] == MERGED_INSTANCE
+
+
+def test_wide_bvh_collapse_fills_nodes():
+    """The SAH dynamic-programming collapse fills the wide nodes: on a
+    displaced icosphere (merged BLAS of 16 untransformed meshes) the nodes
+    average more than five children, where a greedy largest-area expansion
+    leaves most nodes near the leaves with two."""
+    from pathtracer import scenes
+    sd = scenes.icosphere_scene(freq=40, width=32, height=32)
+    nodes, tris, insts, info = collapse(sd)
+    meta = nodes[:, 6:8].copy().view(np.uint8).reshape(-1, 8)
+    children = (meta != 0).sum(1)
+    blas = children[: info["tlas_first"]]
+    assert blas.mean() > 5.0, blas.mean()
+    assert (blas == 2).mean() < 0.2
+    assert tris.shape[0] == 20 * 40 * 40
