@@ -370,6 +370,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=2,
                     help="steps of the 64-job batched workload (p50/p99 job latency, aggregate Mrays/s; 0: skip)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
+    ap.add_argument("--gpu-bvh", action="store_true",
+                    help="build the BVH on the GPU (pt_create_gpu_bvh) instead of collapsing the host-built one")
     ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
@@ -394,7 +396,7 @@ def main():
     build.build_library()
     sd = make_scene(args.config, cfg, small=args.small)
     spp = cfg["spp"]
-    r = GpuRenderer(sd)
+    r = GpuRenderer(sd, gpu_bvh=args.gpu_bvh)
     r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT if args.integrator == "wavefront" else capi.PT_INTEGRATOR_MEGAKERNEL)
     stream = torch.cuda.Stream()
     r.set_stream(stream.cuda_stream)
@@ -568,6 +570,7 @@ def main():
                        "l2": "flushed before each timed step (512 MiB write)",
                        "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU",
                        "tuning": tuning if tuning else "default",
+                       "bvh": f"built on the GPU in {r.gpu_build_ms():.1f} ms" if args.gpu_bvh else "host collapse",
                        "truncated_paths_per_step": truncated / args.steps},
             "gpu_launches": launches,
             "roofline": roofline,

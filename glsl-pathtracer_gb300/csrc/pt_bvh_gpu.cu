@@ -17,12 +17,12 @@
 //      HPG 2012): keys of different groups share fewer than 32 leading bits,
 //      so every group is one subtree;
 //   4. node boxes bottom-up, the second child to arrive at a node joining
-//      the boxes;
+//      the boxes, then the SAH dynamic program of the host collapse the
+//      same way (k_dp);
 //   5. the 8-wide collapse top-down, one launch per level: each wide node
-//      takes up to eight binary descendants, expanding the one of largest
-//      area first; ranges of at most 3 triangles become leaf slots;
-//      children are placed in octant order and quantised conservatively
-//      (directed rounding);
+//      takes the up to eight binary descendants the program chose; ranges
+//      of at most 3 triangles become leaf slots; children are placed in
+//      octant order and quantised conservatively (directed rounding);
 //   6. the TLAS the same way over the merged BLAS and the transformed
 //      instances' boxes.
 #include <cuda_runtime.h>
@@ -213,6 +213,81 @@ __global__ void k_boxes(const Ref* __restrict__ refs, const int* __restrict__ or
     }
 }
 
+// SAH dynamic program over the binary tree (the host collapse's, bvh8_build.cpp,
+// after Ylitie, Karras and Laine, HPG 2017): c[i] is the least cost of a
+// node's subtree as at most i children of the wide node above, k[i] the
+// children given to its left subtree (0: c[i] = c[i-1]).  Leaves of at most
+// three references cost A * kCostPrim * refs, internal children
+// A * kCostNode + the best eight-way distribution.  Bottom-up like k_boxes.
+constexpr float kCostNode = 1.0f, kCostPrim = 0.3f;
+
+struct Dp {
+    float c[9];
+    int8_t k[9];
+    int np;
+};
+
+__device__ __forceinline__ float box_area(const float* lo, const float* hi) {
+    const float dx = fmaxf(0.0f, hi[0] - lo[0]), dy = fmaxf(0.0f, hi[1] - lo[1]), dz = fmaxf(0.0f, hi[2] - lo[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_dp(const Ref* __restrict__ refs, const int* __restrict__ order, const BinNode* __restrict__ nodes,
+                     const int* __restrict__ node_parent, const int* __restrict__ leaf_parent,
+                     const float* __restrict__ boxes, int n, Dp* dp, int* counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int p = leaf_parent[i];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(counters + p, 1) == 0) return;  // the other child is not done yet
+        __threadfence();
+        const BinNode nd = nodes[p];
+        float cl[2][9];
+        int np = 0;
+        const int ch[2] = {nd.left, nd.right};
+        for (int c = 0; c < 2; ++c) {
+            if (ch[c] < 0) {  // one reference: a leaf child
+                const Ref& r = refs[order[~ch[c]]];
+                const float v = box_area(r.lo, r.hi) * kCostPrim;
+                for (int q = 1; q <= 8; ++q) cl[c][q] = v;
+                np += 1;
+            } else {
+                const volatile Dp* d = dp + ch[c];
+                for (int q = 1; q <= 8; ++q) cl[c][q] = d->c[q];
+                np += d->np;
+            }
+        }
+        const float A = box_area(boxes + 6 * p, boxes + 6 * p + 3);
+        float D[9];
+        int8_t K[9];
+        for (int q = 2; q <= 8; ++q) {
+            D[q] = INFINITY;
+            K[q] = 1;
+            for (int j = 1; j < q; ++j) {
+                const float v = cl[0][j] + cl[1][q - j];
+                if (v < D[q]) { D[q] = v; K[q] = (int8_t)j; }
+            }
+        }
+        Dp out;
+        out.np = np;
+        const float cleaf = np <= 3 ? A * kCostPrim * (float)np : INFINITY;
+        const float cnode = A * kCostNode + D[8];
+        out.c[0] = 0.0f;
+        out.k[0] = out.k[1] = 0;
+        out.c[1] = fminf(cleaf, cnode);
+        for (int q = 2; q <= 8; ++q) {
+            if (D[q] < out.c[q - 1]) { out.c[q] = D[q]; out.k[q] = K[q]; }
+            else { out.c[q] = out.c[q - 1]; out.k[q] = 0; }
+        }
+        out.k[0] = K[8];  // the split of the best eight-way distribution (the wide node made of p)
+        volatile Dp* o = dp + p;
+        for (int q = 0; q <= 8; ++q) { o->c[q] = out.c[q]; o->k[q] = out.k[q]; }
+        o->np = out.np;
+        p = node_parent[p];
+    }
+}
+
 // ------------------------------------------------------------- collapse
 struct Task {
     int bin;          // binary internal node, or -1 for a reference range
@@ -225,6 +300,7 @@ struct CollapseArgs {
     const int* order;      // sorted position -> reference
     const BinNode* nodes;
     const float* boxes;    // binary node boxes
+    const Dp* dp;          // the SAH program (k_dp)
     const float4* verts;
     const int* vidx;
     WideNode* wide;
@@ -289,9 +365,30 @@ __global__ void k_collapse(CollapseArgs A, const Task* __restrict__ tasks, int n
     Kid kids[8];
     int nk = 0;
     if (task.bin >= 0) {
+        // the children the SAH program chose: (node, slots) pairs split by
+        // k[] down to single children (at most 8, so at most 9 on the stack)
         const BinNode nd = A.nodes[task.bin];
-        kid_of_node(A, nd.left, kids[nk++]);
-        kid_of_node(A, nd.right, kids[nk++]);
+        const int k8 = A.dp[task.bin].k[0];
+        int st_node[16], st_i[16], sp = 0;
+        st_node[sp] = nd.right; st_i[sp++] = 8 - k8;
+        st_node[sp] = nd.left; st_i[sp++] = k8;
+        while (sp > 0) {
+            const int node = st_node[--sp];
+            int q = st_i[sp];
+            if (node >= 0) {
+                const Dp& d = A.dp[node];
+                while (q > 1 && d.k[q] == 0) --q;
+                if (q > 1) {
+                    if (sp + 2 > 16) { atomicExch(A.error, 1); return; }
+                    const BinNode cn = A.nodes[node];
+                    st_node[sp] = cn.right; st_i[sp++] = q - d.k[q];
+                    st_node[sp] = cn.left; st_i[sp++] = d.k[q];
+                    continue;
+                }
+            }
+            if (nk >= 8) { atomicExch(A.error, 1); return; }
+            kid_of_node(A, node, kids[nk++]);
+        }
     } else {
         // a range of more than 3 references: up to 8 pieces of <= 3 (as the host collapse)
         const int pieces = min(8, (task.count + 2) / 3);
@@ -303,21 +400,6 @@ __global__ void k_collapse(CollapseArgs A, const Task* __restrict__ tasks, int n
             k.count = min(per, task.first + task.count - f);
             range_box(A, k.first, k.count, k);
         }
-    }
-    // expand the internal child of largest area while slots remain
-    for (;;) {
-        if (nk >= 8) break;
-        int best = -1;
-        float best_area = -1.0f;
-        for (int i = 0; i < nk; ++i)
-            if (kids[i].bin >= 0 && area(kids[i]) > best_area) { best_area = area(kids[i]); best = i; }
-        if (best < 0) break;
-        const BinNode nd = A.nodes[kids[best].bin];
-        Kid a, b;
-        kid_of_node(A, nd.left, a);
-        kid_of_node(A, nd.right, b);
-        kids[best] = a;
-        kids[nk++] = b;
     }
     // node box and octant slots (greedy best direction score)
     float nlo[3], nhi[3];
@@ -492,10 +574,11 @@ struct Pass {
     int* leaf_parent = nullptr;
     float* boxes = nullptr;
     int* counters = nullptr;
+    Dp* dp = nullptr;
     void* temp = nullptr;
     void release() {
         dfree(refs); dfree(ref_group); dfree(gbounds); dfree(keys); dfree(keys2); dfree(idx); dfree(order);
-        dfree(nodes); dfree(node_parent); dfree(leaf_parent); dfree(boxes); dfree(counters);
+        dfree(nodes); dfree(node_parent); dfree(leaf_parent); dfree(boxes); dfree(counters); dfree(dp);
         if (temp) cudaFree(temp);
         temp = nullptr;
     }
@@ -529,6 +612,11 @@ cudaError_t tree(Pass& ps, int n, int num_groups, cudaStream_t s, std::vector<Ta
         GB_CK(cudaGetLastError());
         k_boxes<<<(n + B - 1) / B, B, 0, s>>>(ps.refs, ps.order, ps.nodes, ps.node_parent, ps.leaf_parent, n,
                                               ps.boxes, ps.counters);
+        GB_CK(cudaGetLastError());
+        GB_CK(dalloc(ps.dp, ni));
+        GB_CK(cudaMemsetAsync(ps.counters, 0, sizeof(int) * ni, s));
+        k_dp<<<(n + B - 1) / B, B, 0, s>>>(ps.refs, ps.order, ps.nodes, ps.node_parent, ps.leaf_parent, ps.boxes, n,
+                                           ps.dp, ps.counters);
         GB_CK(cudaGetLastError());
     }
     // group ranges from the sorted keys, and the node covering each
@@ -796,6 +884,7 @@ cudaError_t gpu_build_bvh(const GpuBuildInput& in, GpuBvh& out, cudaStream_t s, 
     A.order = ps.order;
     A.nodes = ps.nodes;
     A.boxes = ps.boxes;
+    A.dp = ps.dp;
     A.verts = in.verts;
     A.vidx = in.vidx;
     A.wide = out.nodes;
@@ -879,6 +968,7 @@ cudaError_t gpu_build_bvh(const GpuBuildInput& in, GpuBvh& out, cudaStream_t s, 
     T.order = ps.order;
     T.nodes = ps.nodes;
     T.boxes = ps.boxes;
+    T.dp = ps.dp;
     T.wide = out.nodes;
     T.insts = out.insts;
     T.tlas_blas_root = d_ir;
