@@ -521,8 +521,10 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
             if (REPLAY && sr.suspended) {
                 shadow = true;  // to the transmittance queue; the path state stays as it was
             } else {
-                store_path<MEDIUM>(B, i, ps);
                 shadow = !INLINE && sr.n != 0;
+                // a path that ends here with no shadow query pending needs
+                // only its radiance (B.rad, below)
+                if (cont || shadow) store_path<MEDIUM>(B, i, ps);
             }
             if (!REPLAY && shadow && MEDIUM == 2) {  // deferred transmittance (wf_transmit)
                 const int bits = sr.n | (sr.adds << 2) | (cont ? 0 : 16);
