@@ -1434,7 +1434,7 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
         best.shadow_refill = rs;
         // 3. triangle postponement (shared by both stages)
         if (postpone) {
-            const int mins[] = {0, 4, 8, 12};
+            const int mins[] = {0, 4, 6, 8, 12};
             float bt = 1e30f;
             int mt = best.min_tris;
             for (int m : mins) {
