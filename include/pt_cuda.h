@@ -259,7 +259,7 @@ int pt_render_tile(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t fram
  * integrator, for callers that must not allocate device memory while they
  * render (code running inside a memory budget fixed up front, or between
  * calls that must not synchronise the device, as cudaMalloc/cudaFree can):
- * the path state lives in one fixed device array of 16384 paths (4.4 MiB,
+ * the path state lives in one fixed device array of 16384 paths (5.5 MiB,
  * part of the loaded library), and tiles are traced in bands of whole rows
  * of at most 16384 pixels, giving the samples pt_render_tile gives.  The
  * first call on a device does a one-time set-up (looks the array up); make
