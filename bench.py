@@ -342,6 +342,7 @@ def batch_bench(steps, flush, n_jobs=64, sequential=True):
             seq_ms += st["kernel_ms"]
             seq_rays += st["closest"] + st["shadow"]
             done.append(seq_ms)
+            r.close()  # its path state (up to 9.5 GB) is not kept for the next job
         res["sequential"] = {"value": seq_rays / (seq_ms / 1000.0) / 1e6, "unit": "Mrays/s", "ms": seq_ms,
                              "latency_ms_p50": float(np.percentile(done, 50)),
                              "latency_ms_p99": float(np.percentile(done, 99)),
