@@ -355,9 +355,12 @@ __device__ __forceinline__ bool trav_can_descend(const Trav& s) {
 // Closest hits: the nearest triangle wins; of triangles at exactly the same
 // distance, the one of smallest (triangle, instance) id, so the result does
 // not depend on the order in which triangles are tested.
-template <bool ANY, bool ALPHA, bool PACKED = false>
+// DIRECT: the scene is one untransformed instance entered directly
+// (Params::direct): traversal never leaves its BLAS, and the TLAS code
+// (instance entry, the return to the TLAS) is compiled out.
+template <bool ANY, bool ALPHA, bool PACKED = false, bool DIRECT = false>
 __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack, Rng* rng, int mode = TRAV_LANE) {
-    const bool in_blas = s.cur_inst >= 0;
+    const bool in_blas = DIRECT || s.cur_inst >= 0;
     if (mode == TRAV_TRIS && !(s.pbits && in_blas)) return TRAV_RUNNING;
     if (s.pbits && in_blas && mode == TRAV_NODES) {
         if (s.ng.y <= 0x00ffffffu) return TRAV_RUNNING;  // nothing to descend into: wait for a triangle step
@@ -431,7 +434,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 if (q > 0) return TRAV_RUNNING;
                 if (s.sp == 0) return TRAV_DONE;
                 const uint2 e = stack[--s.sp];
-                if (e.x == kBlasSentinel) {  // back to the TLAS
+                if (!DIRECT && e.x == kBlasSentinel) {  // back to the TLAS
                     const uint2 pend = stack[--s.sp];
                     s.ng = stack[--s.sp];
                     s.pbase = pend.x;

@@ -260,7 +260,9 @@ __device__ __forceinline__ int refill_target(bool exhausted, int refill) { retur
 // unequal the rays are.
 // Traversal is memory-latency bound: 8 blocks of 128 threads (64 registers)
 // keep 32 warps per SM in flight.
-template <int MINB, bool PACKED, bool BATCH = false>
+// DIRECT (this kernel and wf_shadow): the single-instance form of the
+// traversal (trav_step), chosen at launch when Params::direct is set.
+template <int MINB, bool PACKED, bool BATCH = false, bool DIRECT = false>
 __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
         const int target = refill_target(exhausted, refill);
         do {
             const int mode = min_tris > 0 ? trav_warp_mode(s, tracing, min_tris) : TRAV_LANE;
-            if (tracing && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING)
+            if (tracing && trav_step<false, false, PACKED, DIRECT>(s, P, stack, nullptr, mode) != TRAV_RUNNING)
                 tracing = false;
         } while (__popc(__ballot_sync(0xffffffffu, !tracing)) < target);
     }
@@ -571,7 +573,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
 // sample first, then the light sample), persistent like wf_extend, with the
 // same batched retire / refill.  The deferred form is used only when AnyHit
 // draws no random numbers.
-template <bool ADJ, int MINB, bool PACKED, bool BATCH = false>
+template <bool ADJ, int MINB, bool PACKED, bool BATCH = false, bool DIRECT = false>
 __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int refill, int min_tris, AdjView A) {
     uint2 stack[kStackSize];
     extern __shared__ float sgrad[];
@@ -690,7 +692,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
         while (__popc(__ballot_sync(0xffffffffu, !busy)) < target) {
             const int mode = min_tris > 0 ? trav_warp_mode(s, busy, min_tris) : TRAV_LANE;
             if (busy) {
-                const int st = trav_step<true, false, PACKED>(s, P, stack, nullptr, mode);
+                const int st = trav_step<true, false, PACKED, DIRECT>(s, P, stack, nullptr, mode);
                 if (st != TRAV_RUNNING) {
                     if (stage == 1) occ0 = st == TRAV_HIT;
                     else occ1 = st == TRAV_HIT;
@@ -1221,6 +1223,15 @@ template <bool BATCH = false>
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
     const int g = t.extend_grid_v[t.extend_variant];
     const int b = t.extend_block, r = t.extend_refill, m = t.min_tris;
+    if (!BATCH && p.direct) {
+        switch (t.extend_variant) {
+            case 1: wf_extend<8, true, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            case 2: wf_extend<6, false, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            case 3: wf_extend<6, true, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            default: wf_extend<8, false, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+        }
+        return cudaGetLastError();
+    }
     switch (t.extend_variant) {
         case 1: wf_extend<8, true, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
         case 2: wf_extend<6, false, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
@@ -1245,6 +1256,15 @@ static cudaError_t launch_shadow(const Params& p, const WfView& v, const Wavefro
         return cudaGetLastError();
     }
     const int g = t.shadow_grid_v[t.shadow_variant];
+    if (!ADJ && !BATCH && p.direct) {
+        switch (t.shadow_variant) {
+            case 1: wf_shadow<false, 8, true, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            case 2: wf_shadow<false, 6, false, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            case 3: wf_shadow<false, 6, true, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            default: wf_shadow<false, 8, false, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+        }
+        return cudaGetLastError();
+    }
     switch (t.shadow_variant) {
         case 1: wf_shadow<ADJ, 8, true, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
         case 2: wf_shadow<ADJ, 6, false, BATCH><<<g, b, smem, s>>>(p, v, r, m, A); break;
