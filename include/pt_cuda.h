@@ -56,7 +56,7 @@ extern "C" {
  * of iterations or, on a shared plane, without end.  Every integrator here
  * (and the oracle) ends a path after this many iterations with the radiance
  * gathered so far; pt_stats.truncated_paths counts them. */
-#define PT_MAX_PATH_ITERATIONS 4096
+#define PT_MAX_PATH_ITERATIONS 1024
 
 /* ---- scene description: the reference's flattened host arrays ---------- */
 typedef struct pt_scene_desc {

@@ -6,7 +6,8 @@
 * empty pass ranges and empty ray sets;
 * degenerate (zero-area) triangles and rays along the axes (zero direction
   components);
-* the path-iteration bound: a stack of 5000 blended layers 4e-3 apart
+* the path-iteration bound (PT_MAX_PATH_ITERATIONS, read from the header):
+  a stack of 5000 blended layers 4e-3 apart
   (farther apart than the EPS offset of a pass-through), which every
   camera ray crosses one iteration at a time, ends each path at
   PT_MAX_PATH_ITERATIONS in the oracle, the megakernel and the wavefront
@@ -23,7 +24,15 @@ from test_gpu_parity import classify_mismatch, image_agreement
 
 pytestmark = pytest.mark.gpu
 
-PT_MAX_PATH_ITERATIONS = 4096
+def header_define(name):
+    import os
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    text = open(os.path.join(root, "include", "pt_cuda.h")).read()
+    return int(re.search(r"#define\s+" + name + r"\s+(\d+)", text).group(1))
+
+
+PT_MAX_PATH_ITERATIONS = header_define("PT_MAX_PATH_ITERATIONS")
 
 
 def render_both(sd, passes=2):
@@ -150,6 +159,7 @@ def test_path_iteration_bound(ptlib, orc):
     pass-through keeps the depth) and ends at the bound."""
     from pathtracer import scenes
     layers = 5000
+    assert layers > PT_MAX_PATH_ITERATIONS
     meshes = []
     quad = scenes.quad_mesh((-50, -50, 0), (50, -50, 0), (50, 50, 0), (-50, 50, 0), (0, 0, 1))  # wider than the view
     P = np.concatenate([quad.verts[:, :3] + np.array([0, 0, -4e-3 * k]) for k in range(layers)])
