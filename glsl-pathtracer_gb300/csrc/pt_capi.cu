@@ -1366,10 +1366,10 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
     w.w = c->opts.render_width;
     w.h = c->opts.render_height;
     w.first_pass = 0;
-    // trial frames of at least 2^22 paths: on small images a frame of a few
+    // trial frames of at least 2^23 paths: on small images a frame of a few
     // passes is too short to time the candidates apart
     const long npix = (long)w.w * w.h;
-    w.num_passes = (int)std::max<long>(num_passes, ((1L << 22) + npix - 1) / std::max(npix, 1L));
+    w.num_passes = (int)std::max<long>(num_passes, ((1L << 23) + npix - 1) / std::max(npix, 1L));
     w.tile_frame = -1;
     w.tile_x = w.tile_y = 0;
     const int cap = wavefront_capacity(c, w);
@@ -1385,12 +1385,12 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
     const bool postpone = trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth);
     StageTimer timer;
     int rc = PT_OK;
-    // device time per stage of a frame with tuning t: the faster of two
+    // device time per stage of a frame with tuning t: the fastest of three
     // timed frames after one untimed one
     auto measure = [&](const WavefrontTuning& t, float ms[STAGE_COUNT]) -> int {
         for (int k = 0; k < STAGE_COUNT; ++k) ms[k] = 1e30f;
         Params p = make_params(c);
-        for (int rep = 0; rep < 3; ++rep) {
+        for (int rep = 0; rep < 4; ++rep) {
             timer.reset();
             CK(launch_wavefront(p, w, c->wf, t, false, c->stream, nullptr, rep ? &timer : nullptr));
             if (!rep) continue;

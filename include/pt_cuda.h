@@ -362,7 +362,7 @@ typedef struct pt_tuning {
     float   frame_ms;        /* pt_autotune: device time of the tuned frame */
 } pt_tuning;
 
-/* Autotuner: renders num_passes whole-frame passes (at least 2^22 paths:
+/* Autotuner: renders num_passes whole-frame passes (at least 2^23 paths:
  * more passes on small images) into a scratch accumulation, the context's
  * untouched, with candidate configurations,
  * timing each stage with CUDA events, and keeps the fastest for this scene
