@@ -866,6 +866,10 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.status = b->status.p;
     p.jobs = b->job_table.p;
     p.num_jobs = (int)entries.size();
+    // every job enters its BLAS directly: the direct form of the traversal
+    // kernels (each path still takes its job's root and entry)
+    p.direct = 1;
+    for (const BatchJob& J : base) p.direct &= J.direct;
     p.job_remaining = b->remaining.p;
     p.job_done = b->done.p;
     WavefrontTuning t = b->tuning;

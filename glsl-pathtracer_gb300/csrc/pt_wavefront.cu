@@ -1223,12 +1223,13 @@ template <bool BATCH = false>
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
     const int g = t.extend_grid_v[t.extend_variant];
     const int b = t.extend_block, r = t.extend_refill, m = t.min_tris;
-    if (!BATCH && p.direct) {
+    // a batch takes the direct form when every job enters directly (p.direct)
+    if (p.direct) {
         switch (t.extend_variant) {
-            case 1: wf_extend<8, true, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
-            case 2: wf_extend<6, false, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
-            case 3: wf_extend<6, true, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
-            default: wf_extend<8, false, false, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            case 1: wf_extend<8, true, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            case 2: wf_extend<6, false, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            case 3: wf_extend<6, true, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
+            default: wf_extend<8, false, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
         }
         return cudaGetLastError();
     }
@@ -1256,12 +1257,12 @@ static cudaError_t launch_shadow(const Params& p, const WfView& v, const Wavefro
         return cudaGetLastError();
     }
     const int g = t.shadow_grid_v[t.shadow_variant];
-    if (!ADJ && !BATCH && p.direct) {
+    if (!ADJ && p.direct) {
         switch (t.shadow_variant) {
-            case 1: wf_shadow<false, 8, true, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
-            case 2: wf_shadow<false, 6, false, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
-            case 3: wf_shadow<false, 6, true, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
-            default: wf_shadow<false, 8, false, false, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            case 1: wf_shadow<false, 8, true, BATCH, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            case 2: wf_shadow<false, 6, false, BATCH, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            case 3: wf_shadow<false, 6, true, BATCH, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
+            default: wf_shadow<false, 8, false, BATCH, true><<<g, b, smem, s>>>(p, v, r, m, A); break;
         }
         return cudaGetLastError();
     }

@@ -99,6 +99,35 @@ def test_batch_equals_individual_renders(ptlib, monkeypatch, env):
             r.close()
 
 
+def test_all_direct_batch(ptlib):
+    """Jobs that are all one untransformed instance each (the merged BLAS):
+    the batch runs the direct form of the traversal kernels."""
+    from pathtracer import capi, scenes
+    from pathtracer.renderer import GpuBatch, GpuRenderer
+    jobs = [(scenes.cornell(48, 40, max_depth=4, tile=16), 0, 3),
+            (scenes.icosphere_scene(freq=30, width=40, height=24, max_depth=6, tile=16), 2, 2),
+            (scenes.diff_scene(freq=20, width=32, height=32, max_depth=5), 1, 3)]
+    rs = [GpuRenderer(sd, **COMMON) for sd, _, _ in jobs]
+    try:
+        ref = []
+        for r, (sd, fp, n) in zip(rs, jobs):
+            r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+            r.clear()
+            r.render_passes(fp, n)
+            ref.append(r.accum())
+            r.clear()
+        with GpuBatch(rs) as b:
+            b.render([fp for _, fp, _ in jobs], [n for _, _, n in jobs])
+            st = b.stats()
+        assert st["status"] == 0
+        for r, a in zip(rs, ref):
+            frac, mean_rel = image_agreement(r.accum(), a)
+            assert frac >= 0.999 and mean_rel < 1e-4, (r.width, r.height, frac, mean_rel)
+    finally:
+        for r in rs:
+            r.close()
+
+
 def test_single_job_batch(ptlib):
     from pathtracer import capi
     from pathtracer.renderer import GpuBatch, GpuRenderer
