@@ -55,11 +55,12 @@ __device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
 }
 
 
-// Byte j of w in the low mantissa bits of 2^23 (the float 2^23 + byte),
-// without the (quarter-rate) integer conversion.
+// 2^15 + byte j of w, exactly: the byte in mantissa bits 8-15 of 2^15
+// (where their weight is 1), without the (quarter-rate) integer conversion.
 __device__ __forceinline__ float qbyte_biased(uint32_t w, int j) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j));
+    return __uint_as_float(__byte_perm(w, 0x47000000u, 0x7404u | ((uint32_t)j << 4)));
 }
+constexpr float kQBias = 32768.0f;
 
 // Packed FP32 pairs (sm_100+): one instruction for two IEEE round-to-nearest
 // operations, with the results of the two scalar ones.
@@ -72,18 +73,17 @@ __device__ __forceinline__ unsigned long long f2pack(float lo, float hi) {
 #endif
     return r;
 }
-// ((a - b) * c + d) per lane of the pairs, rounded as fmaf(a - b, c, d)
-__device__ __forceinline__ void f2_sub_fma(unsigned long long a, unsigned long long b, unsigned long long c,
-                                           unsigned long long d, float& lo, float& hi) {
+// a * c + d per lane of the pairs, rounded as fmaf(a, c, d)
+__device__ __forceinline__ void f2_fma(unsigned long long a, unsigned long long c, unsigned long long d, float& lo,
+                                       float& hi) {
 #ifdef __CUDA_ARCH__
-    unsigned long long t, r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(a), "l"(b));
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(t), "l"(c), "l"(d));
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(c), "l"(d));
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
 #else
     auto f = [](unsigned long long v, int k) { return __uint_as_float((uint32_t)(v >> (32 * k))); };
-    lo = fmaf(f(a, 0) - f(b, 0), f(c, 0), f(d, 0));
-    hi = fmaf(f(a, 1) - f(b, 1), f(c, 1), f(d, 1));
+    lo = fmaf(f(a, 0), f(c, 0), f(d, 0));
+    hi = fmaf(f(a, 1), f(c, 1), f(d, 1));
 #endif
 }
 
@@ -107,10 +107,16 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
 }
 
 // Slab test of the eight children of wide node `idx`; returns the hit mask.
-// Plane distances are (q - 2^23 bias) * (scale / d) + (origin - o) / d; the
-// entry and exit distances are three-input max / min (sm_100+).  PACKED
-// computes the near and far planes of an axis as one packed pair (the same
-// values, fewer instructions, more registers).
+// A plane's distance is q * adj + org with q the plane's byte, adj =
+// scale / d and org = (node origin - o) / d.  It is evaluated as one FMA,
+// Q * adj + C, with Q = 2^15 + q (exact, qbyte_biased) and C = org - 2^15 *
+// adj rounded down for near planes and up for far planes.  Rounding is
+// monotonic, so a near distance is never above fl(q * adj + org) and a far
+// distance never below it: the test accepts every box that the two-step
+// form fl((Q - 2^15) * adj + org) accepts, and more only by ulp(C) (about
+// 2^-8 of a quantisation step).  Entry and exit distances are three-input
+// max / min (sm_100+).  PACKED computes the near and far planes of an axis
+// as one packed pair (the same values, fewer instructions, more registers).
 template <bool PACKED = false>
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
                                                    float tmax, uint32_t& child_base, uint32_t& prim_base,
@@ -127,6 +133,9 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
     const float orgx = (__uint_as_float(w0.x) - r.o.x) * r.ix;
     const float orgy = (__uint_as_float(w0.y) - r.o.y) * r.iy;
     const float orgz = (__uint_as_float(w0.z) - r.o.z) * r.iz;
+    const float cnx = __fmaf_rd(-kQBias, adjx, orgx), cfx = __fmaf_ru(-kQBias, adjx, orgx);
+    const float cny = __fmaf_rd(-kQBias, adjy, orgy), cfy = __fmaf_ru(-kQBias, adjy, orgy);
+    const float cnz = __fmaf_rd(-kQBias, adjz, orgz), cfz = __fmaf_ru(-kQBias, adjz, orgz);
     const uint32_t oct_inv4 = r.oct_inv * 0x01010101u;
     const bool nx = !(r.oct_inv & 1u), ny = !(r.oct_inv & 2u), nz = !(r.oct_inv & 4u);
     uint32_t hits = 0;
@@ -146,20 +155,19 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
         for (int j = 0; j < 4; ++j) {
             float tnx, tfx, tny, tfy, tnz, tfz;
             if (PACKED) {
-                const unsigned long long bias = f2pack(8388608.0f, 8388608.0f);
-                f2_sub_fma(f2pack(qbyte_biased(nxw, j), qbyte_biased(fxw, j)), bias, f2pack(adjx, adjx),
-                           f2pack(orgx, orgx), tnx, tfx);
-                f2_sub_fma(f2pack(qbyte_biased(nyw, j), qbyte_biased(fyw, j)), bias, f2pack(adjy, adjy),
-                           f2pack(orgy, orgy), tny, tfy);
-                f2_sub_fma(f2pack(qbyte_biased(nzw, j), qbyte_biased(fzw, j)), bias, f2pack(adjz, adjz),
-                           f2pack(orgz, orgz), tnz, tfz);
+                f2_fma(f2pack(qbyte_biased(nxw, j), qbyte_biased(fxw, j)), f2pack(adjx, adjx), f2pack(cnx, cfx), tnx,
+                       tfx);
+                f2_fma(f2pack(qbyte_biased(nyw, j), qbyte_biased(fyw, j)), f2pack(adjy, adjy), f2pack(cny, cfy), tny,
+                       tfy);
+                f2_fma(f2pack(qbyte_biased(nzw, j), qbyte_biased(fzw, j)), f2pack(adjz, adjz), f2pack(cnz, cfz), tnz,
+                       tfz);
             } else {
-                tnx = fmaf(qbyte_biased(nxw, j) - 8388608.0f, adjx, orgx);
-                tfx = fmaf(qbyte_biased(fxw, j) - 8388608.0f, adjx, orgx);
-                tny = fmaf(qbyte_biased(nyw, j) - 8388608.0f, adjy, orgy);
-                tfy = fmaf(qbyte_biased(fyw, j) - 8388608.0f, adjy, orgy);
-                tnz = fmaf(qbyte_biased(nzw, j) - 8388608.0f, adjz, orgz);
-                tfz = fmaf(qbyte_biased(fzw, j) - 8388608.0f, adjz, orgz);
+                tnx = fmaf(qbyte_biased(nxw, j), adjx, cnx);
+                tfx = fmaf(qbyte_biased(fxw, j), adjx, cfx);
+                tny = fmaf(qbyte_biased(nyw, j), adjy, cny);
+                tfy = fmaf(qbyte_biased(fyw, j), adjy, cfy);
+                tnz = fmaf(qbyte_biased(nzw, j), adjz, cnz);
+                tfz = fmaf(qbyte_biased(fzw, j), adjz, cfz);
             }
             const float t0 = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
             const float t1 = fmin3f(tfx, tfy, fminf(tfz, tmax));
