@@ -20,6 +20,17 @@ LIB = os.path.join(CSRC, "libptgb.so")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
 CU_SOURCES = ["pt_kernels.cu", "pt_wavefront.cu", "pt_capi.cu", "pt_bvh_gpu.cu"]
+# The path-tracing kernels divide and take square roots as a GPU runs GLSL:
+# a / b within 2 ulp and sqrt as the hardware approximation
+# (-prec-div=false -prec-sqrt=false; GLSL allows 2.5 ulp for a / b and
+# defines sqrt through inversesqrt), not the IEEE-rounded results.  The
+# shading stage takes a third less time.  Hits do not depend on it: the
+# triangle test and the ray-origin offsets use explicitly rounded
+# operations (__fdiv_rn, __fmul_rn, __fmaf_rn ...), which no flag changes;
+# the slab test's reciprocal ray direction may differ in its last bits,
+# which moves the tested box bounds by as little.
+_GLSL_PRECISION = ["-prec-div=false", "-prec-sqrt=false"]
+FILE_FLAGS = {"pt_kernels.cu": _GLSL_PRECISION, "pt_wavefront.cu": _GLSL_PRECISION}
 CPP_SOURCES = ["bvh8_build.cpp", "cuda_renderer.cpp"]
 
 
@@ -57,10 +68,10 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags: list[
             continue
         obj = os.path.join(OBJ, src + ".o")
         objs.append(obj)
-        if not force and not _stale(obj, [path] + headers):
+        if not force and not _stale(obj, [path, __file__] + headers):
             continue
         if src.endswith(".cu"):
-            cmd = [nv] + NVCC_FLAGS + (extra_flags or []) + ["-c", path, "-o", obj]
+            cmd = [nv] + NVCC_FLAGS + FILE_FLAGS.get(src, []) + (extra_flags or []) + ["-c", path, "-o", obj]
         else:
             cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I/usr/local/cuda/include", "-c", path, "-o", obj]
         jobs.append(cmd)
