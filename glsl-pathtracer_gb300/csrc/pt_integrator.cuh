@@ -187,34 +187,36 @@ __device__ __forceinline__ V3 pow22(float4 t) { return v3(powf(t.x, 2.2f), powf(
 // normal / ffnormal -- and emission), roughness mollification, then ax / ay
 // and eta.
 // The texture-map part of GetMaterial, out of line: scenes without texture
-// maps keep it out of the shading kernels' instruction stream.
-static __device__ __noinline__ void ApplyTextureMaps(const Params& P, int matID, int depth, float prevRough,
-                                                     V3& normal, V3& ffnormal, const Surface& sf, const Ray& r,
-                                                     Material& mat) {
+// maps keep it out of the shading kernels' instruction stream.  The fields
+// of Params it reads come as plain values (see SampleTexArray).
+static __device__ __noinline__ void ApplyTextureMaps(const float4* mats, const uchar4* tex, int tex_w, int tex_h,
+                                                     int num_tex, uint32_t flags, float mollify_amt, int matID,
+                                                     int depth, float prevRough, V3& normal, V3& ffnormal,
+                                                     const Surface& sf, const Ray& r, Material& mat) {
     {
-        const float4 ids = __ldg(P.mats + 8 * matID + 6);  // baseColor, metallicRoughness, normalmap, emission
+        const float4 ids = __ldg(mats + 8 * matID + 6);  // baseColor, metallicRoughness, normalmap, emission
         if ((int)ids.x >= 0) {
-            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.x);
+            const float4 t = SampleTexArray(tex, tex_w, tex_h, num_tex, sf.u, sf.v, ids.x);
             mat.baseColor = mat.baseColor * pow22(t);
             mat.opacity *= t.w;
         }
         if ((int)ids.y >= 0) {
-            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.y);
+            const float4 t = SampleTexArray(tex, tex_w, tex_h, num_tex, sf.u, sf.v, ids.y);
             mat.metallic = t.z;
             mat.roughness = fmaxf(t.y * t.y, 0.001f);
         }
         if ((int)ids.z >= 0) {
-            const float4 t = SampleTexArray(P, sf.u, sf.v, ids.z);
+            const float4 t = SampleTexArray(tex, tex_w, tex_h, num_tex, sf.u, sf.v, ids.z);
             V3 tn = v3(t.x, t.y, t.z);
-            if (P.flags & F_OPENGL_NORMALMAP) tn.y = 1.0f - tn.y;
+            if (flags & F_OPENGL_NORMALMAP) tn.y = 1.0f - tn.y;
             tn = normalize(tn * 2.0f - v3(1.0f));
             const V3 orig = normal;
             normal = normalize(sf.T * tn.x + sf.B * tn.y + normal * tn.z);
             ffnormal = dot(orig, r.direction) <= 0.0f ? normal : -normal;
         }
-        if ((P.flags & F_MOLLIFY) && depth > 0)
-            mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
-        if ((int)ids.w >= 0) mat.emission = pow22(SampleTexArray(P, sf.u, sf.v, ids.w));
+        if ((flags & F_MOLLIFY) && depth > 0)
+            mat.roughness = fmaxf(mixf(0.0f, prevRough, mollify_amt), mat.roughness);
+        if ((int)ids.w >= 0) mat.emission = pow22(SampleTexArray(tex, tex_w, tex_h, num_tex, sf.u, sf.v, ids.w));
     }
 }
 
@@ -222,7 +224,9 @@ __device__ __forceinline__ void GetMaterial(const Params& P, int matID, int dept
                                             V3& ffnormal, const Surface& sf, const Ray& r, Material& mat,
                                             float& eta) {
     LoadMaterial(P.mats, matID, mat);
-    if (P.flags & F_TEXTURES) ApplyTextureMaps(P, matID, depth, prevRough, normal, ffnormal, sf, r, mat);
+    if (P.flags & F_TEXTURES)
+        ApplyTextureMaps(P.mats, P.tex, P.tex_w, P.tex_h, P.num_tex, P.flags, P.mollify_amt, matID, depth, prevRough,
+                         normal, ffnormal, sf, r, mat);
     else if ((P.flags & F_MOLLIFY) && depth > 0)
         mat.roughness = fmaxf(mixf(0.0f, prevRough, P.mollify_amt), mat.roughness);
     FinishMaterial(mat);

@@ -244,12 +244,15 @@ __device__ __forceinline__ V3 xform_point(const float4* __restrict__ xf, int ins
 }
 
 // texture(textureMapsArrayTex, vec3(uv, layer)): bilinear, GL_REPEAT, texel
-// centres at (i + 0.5) / size, the layer rounded and clamped; RGBA8 / 255.
-static __device__ __noinline__ float4 SampleTexArray(const Params& P, float u, float v, float layerf) {
+// centres at (i + 0.5) / size, the layer rounded and clamped; RGBA8 / 255,
+// the UNORM conversion rounded exactly as GL specifies.  The array (tex,
+// w x h texels, n layers) comes as plain values: a reference to Params
+// would make the batch kernels keep their per-job copy of it in memory.
+static __device__ __noinline__ float4 SampleTexArray(const uchar4* tex, int w, int h, int n, float u, float v,
+                                                     float layerf) {
     int layer = (int)floorf(layerf + 0.5f);
-    layer = min(max(layer, 0), P.num_tex - 1);
-    const int w = P.tex_w, h = P.tex_h;
-    const uchar4* base = P.tex + (size_t)layer * w * h;
+    layer = min(max(layer, 0), n - 1);
+    const uchar4* base = tex + (size_t)layer * w * h;
     const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
     const float fx = floorf(x), fy = floorf(y);
     const float ax = x - fx, ay = y - fy;
@@ -262,7 +265,8 @@ static __device__ __noinline__ float4 SampleTexArray(const Params& P, float u, f
     const uchar4 t00 = __ldg(base + (size_t)y0 * w + x0), t10 = __ldg(base + (size_t)y0 * w + x1);
     const uchar4 t01 = __ldg(base + (size_t)y1 * w + x0), t11 = __ldg(base + (size_t)y1 * w + x1);
     auto lerp2 = [&](unsigned char a, unsigned char b, unsigned char c, unsigned char d) {
-        const float ta = (float)a / 255.0f, tb = (float)b / 255.0f, tc = (float)c / 255.0f, td = (float)d / 255.0f;
+        const float ta = __fdiv_rn((float)a, 255.0f), tb = __fdiv_rn((float)b, 255.0f),
+                    tc = __fdiv_rn((float)c, 255.0f), td = __fdiv_rn((float)d, 255.0f);
         const float r0 = ta * (1.0f - ax) + tb * ax;
         const float r1 = tc * (1.0f - ax) + td * ax;
         return r0 * (1.0f - ay) + r1 * ay;
@@ -399,7 +403,8 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                             if (P.flags & F_TEXTURES) {  // the base-colour map's alpha (layer 0 when none)
                                 float tu, tv;
                                 TriTexCoord(P, prim, u, v, w, tu, tv);
-                                opacity *= SampleTexArray(P, tu, tv, __ldg(P.mats + 8 * mat + 6).x).w;
+                                opacity *= SampleTexArray(P.tex, P.tex_w, P.tex_h, P.num_tex, tu, tv,
+                                                          __ldg(P.mats + 8 * mat + 6).x).w;
                             }
                             bool skip = alphaMode == ALPHA_MODE_MASK && opacity < ap.z;
                             if (!skip && alphaMode == ALPHA_MODE_BLEND) skip = rng->next() > opacity;
