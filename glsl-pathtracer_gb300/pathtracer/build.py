@@ -11,8 +11,8 @@ import os
 import shutil
 import subprocess
 
-from .capi import PKG_DIR
-
+# the package root (glsl-pathtracer_gb300/), as pathtracer.capi has it
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG_DIR, "csrc")
 OBJ = os.path.join(CSRC, "_build")
 LIB = os.path.join(CSRC, "libptgb.so")
@@ -82,3 +82,7 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags: list[
     if force or _stale(LIB, objs):
         _run([nv, "-shared", "-gencode", "arch=compute_103a,code=sm_103a"] + objs + ["-o", LIB, "-lcudart"])
     return LIB
+
+
+if __name__ == "__main__":
+    print(build_library(verbose=True))
