@@ -10,8 +10,9 @@
 //   shadow  any-hit queries of the shadow queue, radiance += Ld * T
 // then `resolve` adds each path's radiance into the accumulation buffer,
 // pixel by pixel in pass order, which is the order the megakernel (and the
-// reference's per-pass accumulation, tile.glsl:70-74) adds them in: both
-// forms produce the same accumulation bit for bit.
+// reference's per-pass accumulation, tile.glsl:70-74) adds them in: the two
+// forms' accumulations differ only by the last-bit rounding of their
+// separately compiled shading arithmetic.
 // The stage kernels are persistent grid-stride loops over a device-side
 // count, so a whole batch (generate, max_depth+1 bounces, resolve) needs no
 // host round trip and is captured as one CUDA graph.
