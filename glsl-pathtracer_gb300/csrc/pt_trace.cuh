@@ -326,16 +326,17 @@ enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };
 
 // Work per step in the warp modes (TRAV_NODES / TRAV_TRIS, below), where
 // every lane of a warp does the same kind of step: a triangle step tests a
-// whole leaf child (at most three triangles), and a node step of a
-// closest-hit query goes straight on into the nearest internal child when a
-// visit leaves no triangles pending.  A step's fixed cost (the mode vote,
+// whole leaf child (at most three triangles), and a node step goes
+// straight on into the nearest internal child when a visit leaves no
+// triangles pending (the child the next step would visit, so the order of
+// visits is unchanged).  A step's fixed cost (the mode vote,
 // the loop's ballots, the branch into the node or triangle code) is then
 // paid once per leaf or per two nodes.  Per-lane steps (TRAV_LANE) keep one
 // unit of work: there the node and triangle code of different lanes run one
 // after the other, and longer steps lengthen every divergent iteration
 // (measured on GB300 with the 10k-instance scene).
 constexpr int kTrisPerStep = 3;
-template <bool ANY> constexpr int kNodesPerStep = ANY ? 1 : 2;
+constexpr int kNodesPerStep = 2;
 
 __device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp, uint2 e) {
     if (sp < kStackSize) stack[sp++] = e;
@@ -441,7 +442,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
     // up to kNodesPerStep node visits: after a visit that leaves no triangles
     // pending, the step goes on into the nearest internal child
 #pragma unroll
-    for (int q = 0; q < kNodesPerStep<ANY>; ++q) {
+    for (int q = 0; q < kNodesPerStep; ++q) {
         if (s.next < 0) {
             if (s.ng.y <= 0x00ffffffu) {  // the current group is exhausted: pop
                 if (q > 0) return TRAV_RUNNING;
@@ -482,7 +483,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
         // the next step intersects the nearest child.  (Prefetching it, or the
         // next triangle, into L1 cost more instructions than it saved: the
         // BVH stays in L2, 2.6% on C2.)
-        if (q + 1 == kNodesPerStep<ANY> || mode == TRAV_LANE) return TRAV_RUNNING;
+        if (q + 1 == kNodesPerStep || mode == TRAV_LANE) return TRAV_RUNNING;
     }
     return TRAV_RUNNING;
 }
