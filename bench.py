@@ -148,7 +148,7 @@ class ClockSampler:
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch / its rays, from
 # profiles/wf_extend_wf_shade_wf_shadow_icosphere_1m_1spp.md (traffic grows with the
 # rays of a launch: path-state reads and writes, BVH misses in L2).
-EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 80.0}
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 79.8}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
