@@ -404,7 +404,9 @@ def main():
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     tuning = None
     if args.integrator == "wavefront" and not args.no_autotune:
-        tuning = r.autotune(2)  # set-up, before the timed region
+        # set-up, before the timed region: trial frames of the timed frame's
+        # size, so that the tuning is measured where it is used
+        tuning = r.autotune(spp)
     # each rank renders its own range of sample passes of the same frame
     pass_base = rank * spp * (args.steps + args.warmup + 8)
 
