@@ -197,8 +197,10 @@ int pt_gpu_build_ms(pt_context* ctx, float* ms);
  * several contexts in one wavefront: their device scenes are concatenated
  * once by pt_batch_create (indices re-based), and pt_batch_render traces all
  * jobs' paths through the same persistent kernels, each path carrying its
- * job.  Each job's accumulation buffer receives exactly what
- * pt_render_passes(job, first_pass[j], num_passes[j]) would add.
+ * job.  Each job's accumulation buffer receives what
+ * pt_render_passes(job, first_pass[j], num_passes[j]) would add: the same
+ * paths with the same random numbers, up to the last-bit rounding of the
+ * batch kernels' separately compiled arithmetic.
  * Jobs share one device and their render options' feature flags, and carry
  * surface scenes with analytic lights only (PT_ERR_UNSUPPORTED otherwise:
  * no medium, alpha test, environment map, texture maps or uniform light).
