@@ -32,8 +32,8 @@ segments), counted on the device.
              BVH on a row sample) x the queries of its launches / its own
              launch durations, taken with CUDA events around every launch on
              the launching stream in --stage-steps extra frames; against
-             MEASURED_PEAKS.json.  traffic: DRAM bytes per launch from the
-             ncu capture in profiles/, scaled by the launch's queries.
+             MEASURED_PEAKS.json.  traffic: DRAM bytes per launch from an
+             ncu capture of the same kernel, scaled by the launch's queries.
   cpu_baseline  the oracle (C++ restatement of the reference's shaders, the
              reference's traversal, FP32, OpenMP on all host cores) on a row
              sample of the same frame.
@@ -145,9 +145,10 @@ class ClockSampler:
 
 
 # DRAM bytes per closest-hit query of wf_extend on the icosphere workload:
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch / its rays, from
-# profiles/wf_extend_wf_shade_wf_shadow_icosphere_1m_1spp.md (traffic grows with the
-# rays of a launch: path-state reads and writes, BVH misses in L2).
+# dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch
+# (bounce 0 of a 1-spp frame, 2,073,600 camera rays) / its rays.  Traffic
+# grows with the rays of a launch: path-state reads and writes, BVH misses
+# in L2.
 EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 79.8}
 
 
@@ -201,7 +202,10 @@ def run_reference(args, cfg, name):
     cam = sd.pt_camera()
     import orc
     H = o.render_height
-    step = max(1, H // 16)
+    ncores = os.cpu_count() or 1
+    # at least 8 rows per host thread in every step, so that the dynamic
+    # row schedule keeps all cores busy to the end of the step
+    step = max(1, H // (8 * ncores))
     for _ in range(args.warmup):
         orc.render(sd, o, cam, 0, 1, row_step=H)  # one row
     tot_rays, tot_t = 0, 0.0
@@ -211,7 +215,6 @@ def run_reference(args, cfg, name):
         tot_t += time.perf_counter() - t0
         tot_rays += c["closest"] + c["shadow"]
     v = tot_rays / tot_t / 1e6
-    ncores = os.cpu_count() or 1
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,

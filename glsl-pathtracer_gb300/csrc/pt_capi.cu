@@ -1115,6 +1115,10 @@ int pt_render_tile_noalloc(pt_context* c, int32_t tx, int32_t ty, int32_t frame)
         CK(wavefront_default_tuning(c->wf_tuning, 128));
         c->wf_tuned = true;
     }
+    // Stage timing does not cover this call (its events would be created on
+    // demand); the stage times of an earlier call are dropped, not reported
+    // as this call's.
+    c->timer.reset();
     if (int rc = begin_launch(c)) return rc;
     const Params p = make_params(c);
     const int rows = kFixedScratchPaths / w.w;

@@ -267,10 +267,17 @@ int pt_render_tile(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t fram
  * first call on a device does a one-time set-up (looks the array up); make
  * that call before any stream capture.  Tiles wider than 16384 pixels are
  * rejected with PT_ERR_INVALID_ARG.  The array is shared by every context on
- * the device: calls that overlap in time (other streams, threads or
- * contexts) race on it and must be serialised by the caller.  Nothing in it
- * needs to start at zero.  The context's accumulation buffer is the one
- * pt_render_tile adds to (clear it with pt_clear_accum). */
+ * the device, and the call is asynchronous: it returns once its kernels are
+ * queued on the context's stream.  Work on the array from another stream,
+ * thread or context must therefore be ordered after this call's stream has
+ * finished (a stream synchronise, or an event recorded after the call and
+ * waited on), not merely after the call returns; overlapping work races on
+ * the array and corrupts both renders.  Nothing in it needs to start at
+ * zero.  The context's accumulation buffer is the one pt_render_tile adds
+ * to (clear it with pt_clear_accum).  pt_set_stage_timing does not cover
+ * this call.  The array's address is looked up once per device for the
+ * life of the process; cudaDeviceReset invalidates it together with every
+ * context on that device, so no call may follow a reset. */
 int pt_render_tile_noalloc(pt_context* ctx, int32_t tile_x, int32_t tile_y, int32_t frame_num);
 
 /* Replaces: the material re-upload of Renderer::Update's instancesModified
