@@ -164,10 +164,18 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(REF_DIR, "ref_scene_dump"))
 
 
+def _ref_lib(name: str):
+    """A reference build under _ref/, compiled on first use (make names the
+    macro set from the file name: see the Makefile)."""
+    path = os.path.join(REF_DIR, name)
+    if not os.path.exists(path):
+        subprocess.run(["make", "-C", HERE, os.path.join("_ref", name)], check=True, stdout=subprocess.DEVNULL)
+    return C.CDLL(path)
+
+
 def ref_glsl(variant: str):
     """The reference shaders compiled with feature-macro set `variant`."""
-    path = os.path.join(REF_DIR, f"libref_glsl_{variant}.so")
-    L = C.CDLL(path)
+    L = _ref_lib(f"libref_glsl_{variant}.so")
     P = C.c_void_p
     L.ref_glsl_variant.restype = C.c_char_p
     L.ref_glsl_render.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, P]
@@ -190,29 +198,134 @@ def ref_dump_scene(scene_file: str, out_prefix: str):
                    stdout=subprocess.DEVNULL)
 
 
-def variant_for(scene, options) -> str:
-    """Feature-macro set Renderer::InitShaders would compile for this scene
-    (Renderer.cpp:400-476), as one of the variants the Makefile builds."""
+def ref_macros(scene, options) -> list[str]:
+    """The OPT_* macros Renderer::InitShaders injects for this scene and
+    these options (Renderer.cpp:400-476), in its order."""
     mats = scene.materials
-    alpha = bool((mats[:, 29].astype(int) != 0).any())
-    medium = bool((mats[:, 18].astype(int) != 0).any())
-    env = bool(options.enable_envmap) and scene.envmap_rgb is not None
-    lights = scene.lights.shape[0] > 0
-    vm = bool(options.enable_volume_mis)
-    key = (env, lights, alpha, medium, vm, bool(options.enable_rr))
-    table = {
-        (False, True, False, False, False, True): "lights",
-        (False, True, False, False, True, True): "lights",
-        (False, True, False, False, False, False): "lights_norr",
-        (True, True, False, False, False, True): "env",
-        (True, False, False, False, False, True): "envonly",
-        (False, True, True, True, True, True): "volmis",
-        (False, True, True, True, False, True): "vol",
-        (True, True, True, True, True, True): "envvolmis",
-        (False, True, True, False, False, True): "alpha",
-        (False, True, False, True, True, True): "volmis_opaque",
-        (True, True, False, True, True, True): "envvolmis_opaque",
-    }
-    if key not in table:
-        raise KeyError(f"no reference shader variant built for {key}")
-    return table[key]
+    m = []
+    if options.enable_envmap and scene.envmap_rgb is not None:
+        m.append("ENVMAP")
+    if scene.lights.shape[0] > 0:
+        m.append("LIGHTS")
+    if options.enable_rr:
+        m += ["RR", f"RR_DEPTH_{int(options.rr_depth)}"]
+    if options.enable_uniform_light:
+        m.append("UNIFORM_LIGHT")
+    if options.opengl_normal_map:
+        m.append("OPENGL_NORMALMAP")
+    if options.hide_emitters:
+        m.append("HIDE_EMITTERS")
+    if options.enable_background:
+        m.append("BACKGROUND")
+    if options.transparent_background:
+        m.append("TRANSPARENT_BACKGROUND")
+    if (mats[:, 29].astype(int) != 0).any():
+        m.append("ALPHA_TEST")
+    if options.enable_roughness_mollification:
+        m.append("ROUGHNESS_MOLLIFICATION")
+    if (mats[:, 18].astype(int) != 0).any():
+        m.append("MEDIUM")
+    if options.enable_volume_mis:
+        m.append("VOL_MIS")
+    return m
+
+
+# Macro sets that have a short name in the Makefile (the first golden
+# fixtures were made with these).
+_NAMED_VARIANTS = {
+    "lights": "LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP",
+    "lights_norr": "LIGHTS OPENGL_NORMALMAP",
+    "env": "ENVMAP LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP",
+    "envonly": "ENVMAP RR RR_DEPTH_2 OPENGL_NORMALMAP",
+    "volmis": "LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP ALPHA_TEST MEDIUM VOL_MIS",
+    "vol": "LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP ALPHA_TEST MEDIUM",
+    "envvolmis": "ENVMAP LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP ALPHA_TEST MEDIUM VOL_MIS",
+    "alpha": "LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP ALPHA_TEST",
+    "volmis_opaque": "LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP MEDIUM VOL_MIS",
+    "envvolmis_opaque": "ENVMAP LIGHTS RR RR_DEPTH_2 OPENGL_NORMALMAP MEDIUM VOL_MIS",
+}
+
+
+def variant_for(scene, options) -> str:
+    """Name of the reference shader build with the macro set
+    Renderer::InitShaders would compile for this scene (Renderer.cpp:400-476):
+    a short name where the Makefile has one, else o.<MACRO>.<MACRO>...
+    (built on first use).  OPT_VOL_MIS only acts together with OPT_MEDIUM
+    (pathtrace.glsl:118,177,244), so without a medium it is left out."""
+    m = ref_macros(scene, options)
+    if "VOL_MIS" in m and "MEDIUM" not in m:
+        m.remove("VOL_MIS")
+    key = " ".join(m)
+    for name, macros in _NAMED_VARIANTS.items():
+        if macros == key:
+            return name
+    return "o." + ".".join(m)
+
+
+def ref_tonemap(accum, num_samples, options, width, height):
+    """The reference's tonemap.glsl on an accumulation (H x W x 4, bottom row
+    first) with the tonemap uniforms of these options; returns its float
+    output (H x W x 4) before the RGBA8 read-back."""
+    bg = "BACKGROUND" if options.enable_background else "NONE"
+    if options.transparent_background:
+        bg = "TRANSPARENT_BACKGROUND" if not options.enable_background else "BACKGROUND.TRANSPARENT_BACKGROUND"
+    L = _ref_lib(f"libref_tonemap_o.{bg}.so")
+    P = C.c_void_p
+    L.ref_tonemap.argtypes = [P, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, C.c_int, P, P]
+    acc = np.ascontiguousarray(accum, np.float32)
+    out = np.zeros((height, width, 4), np.float32)
+    bgc = np.asarray(list(options.background_col), np.float32)
+    L.ref_tonemap(_p(acc), width, height, np.float32(1.0) / np.float32(num_samples), int(options.enable_tonemap),
+                  int(options.enable_aces), int(options.simple_aces_fit), _p(bgc), _p(out))
+    return out
+
+
+def tonemap(accum, num_samples, options):
+    """tonemap.glsl:97-133 restated in numpy FP32 (test infrastructure): the
+    reference's float output for an accumulation (H x W x 4, bottom row
+    first), before the RGBA8 read-back.  Pinned against the reference's own
+    tonemap.glsl by tests/test_oracle_golden.py."""
+    f32 = np.float32
+    col = np.asarray(accum, f32) * (f32(1.0) / f32(num_samples))  # texture() * invSampleCounter (:99)
+    c = col[..., :3].copy()
+    alpha = col[..., 3]
+    if options.enable_tonemap:
+        if options.enable_aces:
+            if options.simple_aces_fit:  # ACES (:79-88)
+                a, b, y, d, e = f32(2.51), f32(0.03), f32(2.43), f32(0.59), f32(0.14)
+                c = np.clip((c * (a * c + b)) / (c * (y * c + d) + e), f32(0), f32(1))
+            else:  # ACESFitted (:64-77): row vector times the matrices whose columns are listed
+                mi = np.array([[0.59719, 0.35458, 0.04823], [0.07600, 0.90834, 0.01566],
+                               [0.02840, 0.13383, 0.83777]], f32)
+                mo = np.array([[1.60475, -0.53108, -0.07367], [-0.10208, 1.10813, -0.00605],
+                               [-0.00327, -0.07276, 1.07602]], f32)
+
+                def vm(v, m):
+                    return np.stack([(v[..., 0] * m[j, 0] + v[..., 1] * m[j, 1]) + v[..., 2] * m[j, 2]
+                                     for j in range(3)], -1).astype(f32)
+                v = vm(c, mi)
+                a = v * (v + f32(0.0245786)) - f32(0.000090537)  # RRTAndODTFit (:57-62)
+                b = v * (f32(0.983729) * v + f32(0.4329510)) + f32(0.238081)
+                c = np.clip(vm(a / b, mo), f32(0), f32(1))
+        else:  # Tonemap(c, 1.5) (:90-93)
+            lum = (f32(0.212671) * c[..., 0] + f32(0.715160) * c[..., 1]) + f32(0.072169) * c[..., 2]
+            c = c * f32(1.0) / (f32(1.0) + lum / f32(1.5))[..., None]
+    c = np.power(c, f32(1.0 / 2.2)).astype(f32)  # :110
+    H, W = c.shape[:2]
+    out_alpha = np.ones((H, W), f32)
+    bgc = np.broadcast_to(np.asarray(list(options.background_col), f32), c.shape)
+    if options.transparent_background:  # :115-120
+        out_alpha = alpha
+        fy, fx = np.meshgrid(np.arange(H, dtype=f32) + f32(0.5), np.arange(W, dtype=f32) + f32(0.5), indexing="ij")
+        m = np.mod(np.floor(fx / f32(10)) + np.floor(fy / f32(10)), f32(2))
+        res = np.maximum(np.sign(m), f32(0))[..., None]
+        bgc = f32(0.1) * (f32(1) - res) + f32(0.2) * res
+    if options.enable_background or options.transparent_background:  # mix(bgCol, color, alpha) (:122-124)
+        c = bgc * (f32(1) - alpha[..., None]) + c * alpha[..., None]
+    return np.concatenate([c, out_alpha[..., None]], -1).astype(f32)
+
+
+def to_rgba8(x):
+    """The float -> RGBA8 conversion of GetOutputBuffer's read-back: clamp to
+    [0, 1], scale by 255, round to nearest."""
+    return np.floor(np.clip(x, 0, 1) * np.float32(255) + np.float32(0.5)).astype(np.uint8)

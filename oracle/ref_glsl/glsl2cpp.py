@@ -10,6 +10,7 @@ The rewrite is mechanical; the shader code itself is left as written:
     (GLSL's order; C++ leaves it unspecified)
   * tile.glsl: ``#version``, ``#include`` and the ``in``/``out`` interface
     lines are dropped and ``main`` becomes ``tile_main``
+  * tonemap.glsl: likewise, and ``main`` becomes ``tonemap_main``
 Usage: python glsl2cpp.py <shader_dir> <out_dir>
 """
 import os
@@ -28,6 +29,7 @@ FILES = [
     "common/lambert.glsl",
     "common/pathtrace.glsl",
     "tile.glsl",
+    "tonemap.glsl",
 ]
 
 
@@ -41,6 +43,12 @@ def rewrite(text: str, name: str) -> str:
             if s in ("out vec4 color;", "in vec2 TexCoords;"):
                 continue
             line = line.replace("void main(void)", "void tile_main()")
+        if name == "tonemap.glsl":
+            if s.startswith("#version") or s.startswith("#include"):
+                continue
+            if s in ("out vec4 outCol;", "in vec2 TexCoords;"):
+                continue
+            line = line.replace("void main()", "void tonemap_main()")
         if s.startswith("uniform "):
             line = line.replace("uniform ", "", 1)
         if s == "uvec4 seed;":

@@ -177,7 +177,14 @@ inline mat3 make_mat3(const mat4& a) {
     for (int c = 0; c < 3; ++c) for (int k = 0; k < 3; ++k) r.m[c][k] = a.m[c][k];
     return r;
 }
-#define mat3(x) make_mat3(x)
+// mat3(c0, c1, c2): three column vectors (tonemap.glsl's ACES matrices)
+inline mat3 make_mat3(const vec3& c0, const vec3& c1, const vec3& c2) {
+    mat3 r;
+    const vec3* c[3] = {&c0, &c1, &c2};
+    for (int i = 0; i < 3; ++i) { r.m[i][0] = c[i]->x; r.m[i][1] = c[i]->y; r.m[i][2] = c[i]->z; }
+    return r;
+}
+#define mat3(...) make_mat3(__VA_ARGS__)
 // mat * vec: sum taken in column order
 inline vec4 operator*(const mat4& a, const vec4& v) {
     vec4 r;
@@ -187,6 +194,12 @@ inline vec4 operator*(const mat4& a, const vec4& v) {
 inline vec3 operator*(const mat3& a, const vec3& v) {
     vec3 r;
     for (int k = 0; k < 3; ++k) r.e[k] = (a.m[0][k] * v.x + a.m[1][k] * v.y) + a.m[2][k] * v.z;
+    return r;
+}
+// vec * mat: the row vector times the matrix, component j = dot(v, column j)
+inline vec3 operator*(const vec3& v, const mat3& a) {
+    vec3 r;
+    for (int j = 0; j < 3; ++j) r.e[j] = (v.x * a.m[j][0] + v.y * a.m[j][1]) + v.z * a.m[j][2];
     return r;
 }
 inline mat3 transpose(const mat3& a) {
@@ -258,6 +271,9 @@ inline float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 inline vec2 mix(const vec2& a, const vec2& b, const vec2& t) {
     return vec2(a.x * (1.0f - t.x) + b.x * t.x, a.y * (1.0f - t.y) + b.y * t.y);
 }
+inline float mod(float x, float y) { return x - y * std::floor(x / y); }
+inline float sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+inline vec3 clamp(const vec3& v, float lo, float hi) { return vec3(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi)); }
 inline vec3 mix(const vec3& a, const vec3& b, float t) { return vec3(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t)); }
 inline vec3 min(const vec3& a, const vec3& b) { return vec3(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
 inline vec3 max(const vec3& a, const vec3& b) { return vec3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }

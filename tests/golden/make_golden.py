@@ -12,6 +12,14 @@ Run in a container that has the reference source (path in REF below) after
   ref_scene_textured.npz / ref_render_textured.npz
                          a textured scene of this project's (every texture
                          slot, alpha blend) rendered by the reference
+  feature_scene_<case>.npz / ref_render_features.npz
+                         small scenes of this project's, one per render
+                         option, light type and medium type the reference
+                         decides per scene (Renderer.cpp:400-476), rendered
+                         by the reference shaders with that macro set
+  ref_tonemap.npz        the reference's tonemap.glsl on one accumulation
+                         with every tonemap / background combination
+Usage: python make_golden.py [textured | features]
 """
 from __future__ import annotations
 
@@ -184,9 +192,147 @@ def textured_golden():
     return float(acc[..., :3].mean())
 
 
+def distant_light(direction, emission) -> np.ndarray:
+    """Loader.cpp:198-202: a distant light keeps its position (read as the
+    direction towards the light, sampling.glsl:229-236) and area 0."""
+    L = np.zeros(15, np.float32)
+    L[0:3], L[3:6] = direction, emission
+    L[14] = 2
+    return L
+
+
+# case -> (option overrides, lights, environment map, medium cube: (type,
+# density, color, blended boundary) or None)
+FEATURE_CASES = {
+    "uniform_light": (dict(enable_uniform_light=1, uniform_light_col=(0.3, 0.4, 0.5)), ("quad",), False, None),
+    "uniform_light_env": (dict(enable_uniform_light=1, uniform_light_col=(0.3, 0.4, 0.5)), ("quad",), True, None),
+    "hide_emitters": (dict(hide_emitters=1), ("quad", "sphere"), True, None),
+    "background": (dict(enable_background=1, background_col=(0.2, 0.4, 0.8)), ("quad",), True, None),
+    "transparent_background": (dict(transparent_background=1), ("quad",), False, None),
+    "mollification": (dict(enable_roughness_mollification=1, roughness_mollification_amt=0.7), ("quad",), True,
+                      None),
+    "rr_off": (dict(enable_rr=0, max_depth=6), ("quad",), False, None),
+    "rr_depth_1": (dict(rr_depth=1), ("quad", "sphere"), False, None),
+    "env_only": (dict(envmap_rot=40.0, envmap_intensity=1.5), (), True, None),
+    "distant": (dict(), ("distant", "sphere"), False, None),
+    "distant_only": (dict(), ("distant",), True, None),
+    "absorb": (dict(), ("quad",), False, (1, 0.8, (0.3, 0.6, 0.9), False)),
+    "absorb_volmis": (dict(enable_volume_mis=1), ("quad",), False, (1, 0.8, (0.3, 0.6, 0.9), False)),
+    "emissive": (dict(), ("quad",), False, (3, 0.5, (0.5, 0.8, 1.0), True)),
+    "emissive_volmis": (dict(enable_volume_mis=1), ("quad", "sphere"), True, (3, 0.5, (0.5, 0.8, 1.0), False)),
+    "all_flags": (dict(hide_emitters=1, enable_background=1, enable_uniform_light=1, rr_depth=1,
+                       enable_roughness_mollification=1, roughness_mollification_amt=0.5, opengl_normal_map=0),
+                  ("quad",), False, None),
+}
+FEATURE_SIZE = dict(render_width=48, render_height=36, tile_width=24, tile_height=18, max_depth=5)
+FEATURE_PASSES = 4
+
+
+def feature_scene(case):
+    """Ground quad, a glossy clear-coated sphere, a glass sphere, a cube (a
+    medium boundary in the medium cases, else diffuse), an emissive quad in
+    view and the case's lights: a rect light facing the camera from behind
+    the objects, a sphere light, a distant light."""
+    over, lights, env, medium = FEATURE_CASES[case]
+    V, Fc, _ = scenes.icosphere(5, 1.0, 0.0, 1)
+    meshes = [scenes.quad_mesh((-5, 0, -5), (-5, 0, 5), (5, 0, 5), (5, 0, -5), (0, 1, 0)),
+              scenes.mesh_from_indexed(V, Fc), scenes.cube_mesh(),
+              scenes.quad_mesh((-0.4, 0, 0), (0.4, 0, 0), (0.4, 0.5, 0), (-0.4, 0.5, 0), (0, 0, 1))]
+    mats = [scenes.material(),
+            scenes.material(color=(0.7, 0.7, 0.7), roughness=0.9),
+            scenes.material(color=(0.9, 0.5, 0.3), metallic=0.7, roughness=0.15, clearcoat=0.6,
+                            clearcoat_gloss=0.8),
+            scenes.material(color=(1, 1, 1), spec_trans=1.0, roughness=0.02, ior=1.45),
+            scenes.material(color=(0.4, 0.6, 0.3), roughness=0.6, sheen=0.5),
+            scenes.material(color=(0.8, 0.8, 0.8), emission=(3.0, 2.5, 2.0))]
+    if medium is not None:
+        mtype, dens, mcol, blend = medium
+        mats[4] = scenes.material(color=(1, 1, 1), spec_trans=1.0, roughness=0.0, ior=1.0 if blend else 1.2,
+                                  medium_type=mtype, medium_density=dens, medium_color=mcol,
+                                  alpha_mode=1 if blend else 0, opacity=0.0 if blend else 1.0)
+    inst = [(0, 1, scenes.mat4()),
+            (1, 2, scenes.mat4(None, (0.8, 0.8, 0.8), (-1.3, 0.8, 0.0))),
+            (1, 3, scenes.mat4(None, (0.6, 0.6, 0.6), (1.2, 0.6, 0.6))),
+            (2, 4, scenes.mat4(scenes.rot_y(25.0), (1.0, 1.0, 1.0), (0.3, 0.51, -1.3))),
+            (3, 5, scenes.mat4(None, (1, 1, 1), (1.6, 0.0, -2.2)))]
+    lts = []
+    for kind in lights:
+        if kind == "quad":  # faces the camera (+z), behind the objects
+            lts.append(scenes.quad_light((-1.0, 1.2, -3.0), (1.0, 1.2, -3.0), (-1.0, 2.2, -3.0), (6.0, 5.5, 5.0)))
+        elif kind == "sphere":
+            lts.append(scenes.sphere_light((2.0, 3.0, 2.5), 0.35, (20.0, 18.0, 16.0)))
+        elif kind == "distant":
+            lts.append(distant_light((0.4, 0.8, 0.45), (2.0, 1.9, 1.7)))
+    opts = dict(FEATURE_SIZE)
+    opts.update(over)
+    envmap = scenes.sky_envmap(64, 32, sun_dir=(-0.5, 0.6, 0.2), sun_radius_deg=8.0, sun_intensity=40.0) if env \
+        else None
+    if env:
+        opts["enable_envmap"] = 1
+    cam = scenes.camera((0.0, 1.8, 5.5), (0.0, 0.7, 0.0), 45.0)
+    return scenes.build_scene(meshes, inst, mats, lts, cam, opts, envmap=envmap)
+
+
+def feature_goldens():
+    """One scene per feature case and its reference render; the reference's
+    tonemap.glsl on the background case's accumulation."""
+    out, renders = {}, {}
+    for case in FEATURE_CASES:
+        sd = feature_scene(case)
+        o = sd.render_options()
+        variant = orc.variant_for(sd, o)
+        acc = orc.ref_render(variant, sd, o, sd.pt_camera(), 0, FEATURE_PASSES)
+        sd.save_npz(os.path.join(HERE, f"feature_scene_{case}.npz"))
+        renders[f"{case}_accum"] = acc
+        renders[f"{case}_variant"] = np.frombuffer(variant.encode(), np.uint8)
+        out[case] = (variant, float(acc[..., :3].mean()), float(acc[..., 3].mean()))
+    # the reference's textured scene with DirectX-convention normal maps
+    sd = SceneData.load_npz(os.path.join(HERE, "ref_scene_textured.npz"))
+    sd.options = dict(sd.options, opengl_normal_map=0)
+    o = sd.render_options()
+    variant = orc.variant_for(sd, o)
+    g = np.load(os.path.join(HERE, "ref_render_textured.npz"))
+    o = sd.render_options(render_width=int(g["width"]), render_height=int(g["height"]),
+                          tile_width=int(g["tile_w"]), tile_height=int(g["tile_h"]))
+    sd.options = capi.options_dict(o)
+    acc = orc.ref_render(variant, sd, o, sd.pt_camera(), 0, FEATURE_PASSES)
+    sd.save_npz(os.path.join(HERE, "feature_scene_textured_dx.npz"))
+    renders["textured_dx_accum"] = acc
+    renders["textured_dx_variant"] = np.frombuffer(variant.encode(), np.uint8)
+    out["textured_dx"] = (variant, float(acc[..., :3].mean()), float(acc[..., 3].mean()))
+    np.savez_compressed(os.path.join(HERE, "ref_render_features.npz"), passes=FEATURE_PASSES, **renders)
+    # tonemap.glsl: every tonemap branch with and without (transparent) background
+    acc = renders["background_accum"]
+    H, W = acc.shape[:2]
+    import json
+    tm = {"accum": acc, "samples": FEATURE_PASSES,
+          "cases": np.frombuffer(json.dumps(TONEMAP_CASES).encode(), np.uint8)}
+    for name, kw in TONEMAP_CASES.items():
+        o = capi.make_options(render_width=W, render_height=H, background_col=(0.2, 0.4, 0.8), **kw)
+        tm[name] = orc.ref_tonemap(acc, FEATURE_PASSES, o, W, H)
+    np.savez_compressed(os.path.join(HERE, "ref_tonemap.npz"), **tm)
+    return out
+
+
+TONEMAP_CASES = {
+    "reinhard": dict(enable_tonemap=1),
+    "aces": dict(enable_tonemap=1, enable_aces=1),
+    "aces_simple": dict(enable_tonemap=1, enable_aces=1, simple_aces_fit=1),
+    "none": dict(enable_tonemap=0),
+    "reinhard_background": dict(enable_tonemap=1, enable_background=1),
+    "aces_background": dict(enable_tonemap=1, enable_aces=1, enable_background=1),
+    "reinhard_transparent": dict(enable_tonemap=1, transparent_background=1),
+    "aces_simple_transparent": dict(enable_tonemap=1, enable_aces=1, simple_aces_fit=1, transparent_background=1),
+}
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "textured":
         print("textured golden written", textured_golden())
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "features":
+        for k, v in feature_goldens().items():
+            print(k, v)
         return
     if not orc.ref_available():
         raise SystemExit("oracle/_ref not built: run `make -C oracle ref` first")
@@ -233,6 +379,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_closest.npz"),
                         **{f"{k}_{f}": v for k, r in res.items() for f, v in r.items()})
     out["textured"] = textured_golden()
+    out["features"] = feature_goldens()
     print("golden fixtures written", out)
 
 

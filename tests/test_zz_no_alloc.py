@@ -64,3 +64,44 @@ def test_noalloc_rejects_tiles_wider_than_its_scratch(ptlib):
         r.lib.pt_last_error(buf, 256)
         assert b"16384" in buf.value
         assert r.lib.pt_render_tile_noalloc(r.ctx, 1, 0, 2) == capi.PT_ERR_INVALID_ARG  # tile out of range
+
+
+def _free_device_bytes():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info(0)[0]
+
+
+@pytest.mark.parametrize("scene", ["cornell", "volume-replay"])
+def test_noalloc_leaves_device_memory_unchanged(ptlib, scene):
+    """The property the entry point exists for: on a fresh context that only
+    ever calls pt_render_tile_noalloc, the device's free memory is the same
+    before and after several renders.  A warm-up pass comes first, since the
+    first launch of a kernel may load its code onto the device.  The
+    volume scene (blended medium boundary, VOL_MIS, environment map and a
+    light) takes the suspend-and-replay transmittance stage and the tail
+    kernel, whose buffers also live in the fixed array.  The first of three
+    passes is the warm-up; the other two are measured."""
+    from pathtracer import capi, scenes
+    from pathtracer.renderer import GpuRenderer
+    from test_gpu_volume_stages import volume_scene
+    if scene == "cornell":
+        sd, tw, th = scenes.cornell(200, 136), 160, 128
+    else:
+        sd, tw, th = volume_scene(blend=True, env=True, width=96, height=64), 48, 64
+    W, H = sd.render_options().render_width, sd.render_options().render_height
+    with GpuRenderer(sd, tile_width=tw, tile_height=th) as r:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        tiles = _tiles_in_order(W, H, tw, th, 3)
+        per_pass = len(tiles) // 3
+        for tx, ty, frame in tiles[:per_pass]:  # warm-up: the first pass
+            capi.check(r.lib, r.lib.pt_render_tile_noalloc(r.ctx, tx, ty, frame))
+        before = _free_device_bytes()
+        for tx, ty, frame in tiles[per_pass:]:
+            capi.check(r.lib, r.lib.pt_render_tile_noalloc(r.ctx, tx, ty, frame))
+        after = _free_device_bytes()
+        st = r.stats()
+        acc = r.accum()
+    assert st["status"] == 0, st
+    assert np.isfinite(acc).all() and acc[..., :3].sum() > 0
+    assert after == before, (before, after)
