@@ -150,6 +150,11 @@ class ClockSampler:
 # grows with the rays of a launch: path-state reads and writes, BVH misses
 # in L2.
 EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 79.8}
+# Warp-level instructions executed per closest-hit query by wf_extend on the
+# same ncu capture (smsp__inst_executed.sum of the launch / its rays): the
+# numerator of the instruction-issue roofline (4 warp instructions per cycle
+# per SM).
+EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 228.0}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
@@ -163,9 +168,28 @@ def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
     nc, tc = c["nodes"] - c["nodes_any"], c["tris"] - c["tris_any"]
     b_closest = (36.0 * nc + 60.0 * tc + 176.0 * c["tri_hits"]) / max(c["closest"], 1)
     b_shadow = (36.0 * c["nodes_any"] + 60.0 * c["tris_any"]) / max(c["shadow"], 1)
+    # FP32 work of a query: 12 FLOPs per slab test, two per interior node;
+    # 27 per triangle test; 600 per shaded hit
+    f = (24.0 * c["inner"] + 27.0 * c["tris"] + 600.0 * c["tri_hits"]) / max(rays, 1)
     return b, dict(nodes_per_ray=c["nodes"] / rays, tris_per_ray=c["tris"] / rays,
-                   hits_per_ray=c["tri_hits"] / rays, rays=rays, bytes_per_closest_ray=b_closest,
-                   bytes_per_shadow_ray=b_shadow)
+                   hits_per_ray=c["tri_hits"] / rays, inner_nodes_per_ray=c["inner"] / rays, rays=rays,
+                   bytes_per_closest_ray=b_closest, bytes_per_shadow_ray=b_shadow, flops_per_ray=f)
+
+
+def fp32_peak_tflops():
+    """Nominal FP32 rate of the device: SMs x 128 FP32 lanes x 2 (FMA) x the
+    maximum SM clock (MEASURED_PEAKS.json, else the device's own figure)."""
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    mhz = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            mhz = float(json.load(fh)["sm_max_mhz"])
+    except Exception:
+        pass
+    if not mhz:
+        mhz = float(getattr(props, "clock_rate", 2070000)) / 1000.0
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12, props.multi_processor_count, mhz
 
 
 def cpu_baseline(scene, options, camera, spp, target_s=15.0):
@@ -334,6 +358,19 @@ def batch_bench(steps, flush, n_jobs=64, sequential=True):
                 "ms_per_step": statistics.mean(ms), "rays_per_step": rays / steps,
                 "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
                 "latency_ms_max": float(max(lat)), "gpu_launches_per_step": launches / steps})
+    # the batch kernels' per-job cost on its own: the largest job alone, as
+    # a batch of one and through its own pt_render_passes (same paths)
+    one = {}
+    with GpuBatch([rs[big]]) as b1:
+        for k in range(2):
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize()
+            b1.render([spp[big] * (steps + 1)], [spp[big]])
+            one["batch_of_one_ms"] = b1.stats()["kernel_ms"]
+            rs[big].render_passes(spp[big] * (steps + 1), spp[big])
+            one["render_passes_ms"] = rs[big].stats()["kernel_ms"]
+    one["job"] = {"tris": 20 * jobs[big][0] ** 2, "resolution": jobs[big][1], "spp": spp[big], "depth": jobs[big][3]}
+    res["largest_job_alone"] = one
     if sequential:
         # the same jobs one after another, each its own pt_render_passes
         flush.fill_(0)
@@ -355,6 +392,31 @@ def batch_bench(steps, flush, n_jobs=64, sequential=True):
     return res
 
 
+def drop_in_bench(sd, spp, steps, warmup):
+    """The drop-in class, ptgb::CudaRenderer, driven from C++ as the
+    reference's Main.cpp drives GLSLPT::Renderer (tests/cpp/dropin_driver.cpp,
+    constructed from a GLSLPT::Scene*): autotune, then per step RenderPasses
+    of `spp` passes, the Update that completes them and GetOutputBuffer
+    (RGBA8 into a new[] host buffer); wall clock of the timed steps."""
+    import tempfile
+    from pathtracer import build
+    csrc = os.path.dirname(build.LIB)
+    with tempfile.TemporaryDirectory() as td:
+        exe = os.path.join(td, "dropin_driver")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I/usr/local/cuda/include",
+                        os.path.join(ROOT, "tests", "cpp", "dropin_driver.cpp"), "-L" + csrc, "-lptgb",
+                        "-Wl,-rpath," + csrc, "-o", exe], check=True)
+        scene_file = os.path.join(td, "scene.bin")
+        sd.save_flat(scene_file)
+        r = subprocess.run([exe, scene_file, "bench", str(spp), str(steps), str(warmup)], check=True,
+                           capture_output=True, text=True)
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return {"value": d["rays"] / d["seconds"] / 1e6, "unit": "Mrays/s", "steps": d["steps"],
+            "ms_per_step": 1000.0 * d["seconds"] / d["steps"], "h2d_bytes_per_step": 0,
+            "d2h_bytes_per_step": d["d2h_bytes_per_step"],
+            "path": "ptgb::CudaRenderer(GLSLPT::Scene*): RenderPasses + Update + GetOutputBuffer per step"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -373,6 +435,8 @@ def main():
                     help="extra steps timed per kernel with CUDA events (roofline of the dominant kernel)")
     ap.add_argument("--batch-steps", type=int, default=2,
                     help="steps of the 64-job batched workload (p50/p99 job latency, aggregate Mrays/s; 0: skip)")
+    ap.add_argument("--drop-in-steps", type=int, default=5,
+                    help="timed steps of the C++ drop-in class on the same frame (0: skip)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
     ap.add_argument("--gpu-bvh", action="store_true",
                     help="build the BVH on the GPU (pt_create_gpu_bvh) instead of collapsing the host-built one")
@@ -533,6 +597,10 @@ def main():
            "h2d_bytes_per_step": C.sizeof(capi.pt_camera),
            "d2h_bytes_per_step": int(r.width * r.height * 4)}
 
+    drop_in = None
+    if args.drop_in_steps > 0 and rank == 0 and args.integrator == "wavefront":
+        drop_in = drop_in_bench(sd, spp, args.drop_in_steps, args.warmup)
+
     line = None
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -559,11 +627,29 @@ def main():
             traffic = None
             if dom == "wf_extend" and args.config in EXTEND_DRAM_BYTES_PER_RAY and not args.small:
                 traffic = EXTEND_DRAM_BYTES_PER_RAY[args.config] * kd["rays_per_launch"]
+            # secondary rooflines of the frame: FP32 work (algorithmic FLOPs
+            # per query, against the nominal FP32 rate) and instruction
+            # issue of the dominant kernel (ncu's instructions per query)
+            fpk, nsm, mhz = fp32_peak_tflops()
+            f_ach = work["flops_per_ray"] * rays_per_step / (mean_ms / 1000.0) / 1e12
+            fp32 = {"achieved": f_ach, "peak": fpk, "unit": "TFLOP/s", "frac": f_ach / fpk,
+                    "flops_per_ray": work["flops_per_ray"],
+                    "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz"}
+            issue = None
+            if dom == "wf_extend" and args.config in EXTEND_WARP_INST_PER_RAY and not args.small:
+                ipr = EXTEND_WARP_INST_PER_RAY[args.config]
+                i_ach = ipr * kd["rays_per_launch"] / (kd["avg_launch_ms"] / 1000.0) / 1e12
+                i_peak = nsm * 4 * mhz * 1e6 / 1e12
+                issue = {"kernel": dom, "achieved": i_ach, "peak": i_peak, "unit": "Twarp-inst/s",
+                         "frac": i_ach / i_peak, "warp_inst_per_ray": ipr,
+                         "dram_bytes_per_ray": EXTEND_DRAM_BYTES_PER_RAY.get(args.config),
+                         "peak_source": f"nominal: {nsm} SMs x 4 schedulers x {mhz:.0f} MHz"}
             roofline = {"bound": "hbm", "kernel": dom, "achieved": kd["achieved"], "peak": peak, "unit": "GB/s",
                         "frac": kd["achieved"] / peak, "traffic": traffic,
                         "algorithmic_bytes_per_launch": kd["bytes_per_ray"] * kd["rays_per_launch"],
                         "peak_source": peak_kind, "kernels": kernels,
-                        "frame": {"achieved": achieved, "frac": achieved / peak, "bytes_per_ray": b_ray}, **work}
+                        "frame": {"achieved": achieved, "frac": achieved / peak, "bytes_per_ray": b_ray},
+                        "fp32": fp32, "issue": issue, **work}
         cpu = None
         if not args.no_cpu_baseline:
             cpu, _, _ = cpu_baseline(sd, sd.render_options(), cam, spp)
@@ -588,6 +674,8 @@ def main():
                               "launches_per_step": {k: v / stages["steps"] for k, v in stages["launches"].items()}}
         if other:
             line["compare"] = other
+        if drop_in:
+            line["e2e_drop_in"] = drop_in
         if adjoint:
             line["adjoint"] = adjoint
         if batch:

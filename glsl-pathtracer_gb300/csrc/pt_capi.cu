@@ -109,6 +109,10 @@ struct pt_context {
     int launches = 0;  // kernels launched by the last render call
     bool stage_timing = false;
     StageTimer timer;
+    // traversal stack bound of the kernels: kStackSize, or lower when
+    // PT_TRAVERSAL_STACK_LIMIT is set at pt_create (failure-detection tests
+    // make the overflow status fire with it)
+    int stack_limit = kStackSize;
     // scene / camera / options version, and the forward wavefront batch the
     // path buffers hold (the adjoint reuses its per-path radiance)
     uint64_t version = 1;
@@ -197,6 +201,7 @@ Params make_params(const pt_context* c) {
     p.accum = c->accum.p;
     p.counters = c->counters.p;
     p.status = c->status.p;
+    p.stack_limit = c->stack_limit;
     return p;
 }
 
@@ -251,9 +256,10 @@ int upload_bvh(pt_context* c) {
     CK(c->insts.upload(c->bvh.insts, c->bvh.num_inst_refs, c->stream));
     c->direct = c->bvh.num_inst_refs == 1 && c->bvh.insts[0].identity;
     if (c->direct) c->entry = c->bvh.insts[0];
-    if (c->bvh.tlas_depth + c->bvh.blas_depth > kStackSize)
-        return set_err(PT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" +
-                                               std::to_string(c->bvh.tlas_depth + c->bvh.blas_depth) + " levels)");
+    const int need = trav_stack_need(c->bvh.tlas_depth, c->bvh.blas_depth, c->direct);
+    if (need > kStackSize)
+        return set_err(PT_ERR_UNSUPPORTED, "BVH deeper than the traversal stack (" + std::to_string(need) +
+                                               " entries needed, " + std::to_string(kStackSize) + " available)");
     return PT_OK;
 }
 
@@ -407,7 +413,7 @@ int gpu_rebuild(pt_context* c, const float* transforms) {
         return set_err(e == cudaErrorMemoryAllocation ? PT_ERR_OUT_OF_MEMORY : PT_ERR_INVALID_ARG,
                        "GPU BVH build: " + (err.empty() ? std::string(cudaGetErrorString(e)) : err));
     }
-    if (g.tlas_depth + g.blas_depth + 3 > kStackSize) {
+    if (trav_stack_need(g.tlas_depth, g.blas_depth, false) > kStackSize) {
         g.release();
         return set_err(PT_ERR_UNSUPPORTED, "GPU-built BVH deeper than the traversal stack");
     }
@@ -471,6 +477,8 @@ int create(const pt_scene_desc* d, const pt_mesh_desc* meshes, const pt_render_o
     }
     pt_context* c = new pt_context;
     c->opts = *o;
+    if (const char* e = std::getenv("PT_TRAVERSAL_STACK_LIMIT"))
+        c->stack_limit = std::min(kStackSize, std::max(1, std::atoi(e)));
     int rc = PT_OK;
     do {
         cudaError_t e = cudaGetDevice(&c->device);
@@ -864,6 +872,8 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.mollify_amt = b->jobs[0]->opts.roughness_mollification_amt;
     p.counters = b->counters.p;
     p.status = b->status.p;
+    p.stack_limit = kStackSize;
+    for (pt_context* c : b->jobs) p.stack_limit = std::min(p.stack_limit, c->stack_limit);
     p.jobs = b->job_table.p;
     p.num_jobs = (int)entries.size();
     // every job enters its BLAS directly: the direct form of the traversal
@@ -1244,6 +1254,13 @@ int pt_render_passes(pt_context* c, int32_t first_pass, int32_t num_passes) {
 int pt_get_accum(pt_context* c, float* host) {
     if (!c || !host) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     CK(cudaMemcpyAsync(host, c->accum.p, c->accum.n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+int pt_set_accum(pt_context* c, const float* host) {
+    if (!c || !host) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
+    CK(cudaMemcpyAsync(c->accum.p, host, c->accum.n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return PT_OK;
 }

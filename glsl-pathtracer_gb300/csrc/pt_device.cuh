@@ -124,11 +124,19 @@ struct LightSample { V3 normal, emission, direction; float dist, pdf; };
 struct Light { V3 position, emission, u, v; float radius, area, type; };
 
 // ------------------------------------------------------------- sampling
-// common/sampling.glsl:25-32
-__device__ __forceinline__ float GTR1(float NDotH, float a) {
+// common/sampling.glsl:25-32, of the half vector H in the shading frame.
+// The reference's denominator 1 + (a^2 - 1) (N.H)^2 cancels near the lobe's
+// peak (N.H -> 1, small a): the last bits of N.H then reach the result
+// amplified by 1 / (1 - (N.H)^2), far past 1e-5 relative in FP32.  For a
+// unit H it equals (Hx^2 + Hy^2 + a^2 Hz^2) / |H|^2, a ratio of sums of
+// positive terms that is evaluated here instead: the same function, exact
+// to a few ulp whatever the angle, and free of H's normalisation error.
+__device__ __forceinline__ float GTR1(V3 H, float a) {
     if (a >= 1.0f) return PT_INV_PI;
     float a2 = a * a;
-    float t = 1.0f + (a2 - 1.0f) * NDotH * NDotH;
+    float s = H.x * H.x + H.y * H.y;
+    float z2 = H.z * H.z;
+    float t = (s + a2 * z2) / (s + z2);
     return (a2 - 1.0f) / (PT_PI * logf(a2) * t);
 }
 // sampling.glsl:34-47
@@ -364,7 +372,7 @@ __device__ __forceinline__ V3 EvalClearcoat(const Material& mat, V3 V, V3 L, V3 
     if (L.z <= 0.0f) return v3(0.0f);
     float VDotH = dot(V, H);
     float F = mixf(0.04f, 1.0f, SchlickWeight(VDotH));
-    float D = GTR1(H.z, mat.clearcoatRoughness);
+    float D = GTR1(H, mat.clearcoatRoughness);
     float G = SmithG(L.z, 0.25f) * SmithG(V.z, 0.25f);
     float jacobian = 1.0f / (4.0f * VDotH);
     pdf = D * H.z * jacobian;

@@ -224,10 +224,13 @@ __device__ __forceinline__ MatD<NC> LoadMaterialD(const float4* __restrict__ mat
     return m;
 }
 
-template <int NC> __device__ __forceinline__ D<NC> GTR1D(float NDotH, const D<NC>& a) {  // sampling.glsl:25-32
+// sampling.glsl:25-32 in the cancellation-free form of pt_device.cuh's GTR1
+template <int NC> __device__ __forceinline__ D<NC> GTR1D(V3 H, const D<NC>& a) {
     if (a.v >= 1.0f) return dconst<NC>(PT_INV_PI);
     const D<NC> a2 = a * a;
-    const D<NC> t = 1.0f + (a2 - 1.0f) * (NDotH * NDotH);
+    const float s = H.x * H.x + H.y * H.y;
+    const float z2 = H.z * H.z;
+    const D<NC> t = (s + a2 * z2) * (1.0f / (s + z2));
     return (a2 - 1.0f) / (PT_PI * dlog(a2) * t);
 }
 template <int NC>
@@ -318,7 +321,7 @@ __device__ __forceinline__ DV3<NC> EvalMicrofacetRefractionD(const MatD<NC>& mat
 template <int NC> __device__ __forceinline__ D<NC> EvalClearcoatD(const MatD<NC>& mat, V3 V, V3 L, V3 H) {
     const float VDotH = dot(V, H);
     const float F = mixf(0.04f, 1.0f, SchlickWeight(VDotH));
-    const D<NC> Dd = GTR1D(H.z, mat.clearcoatRoughness);
+    const D<NC> Dd = GTR1D(H, mat.clearcoatRoughness);
     const float G = SmithG(L.z, 0.25f) * SmithG(V.z, 0.25f);
     return Dd * (F * G);
 }

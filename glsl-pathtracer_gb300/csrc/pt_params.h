@@ -12,11 +12,20 @@ namespace ptgb {
 // Traversal stack entries per thread (node groups of the wide BVH; one per
 // wide level on the current path, TLAS + BLAS).
 constexpr int kStackSize = 48;
+// Stack entries of one instance entry: the TLAS node group, the pending
+// instances, the world ray's reciprocal direction and a sentinel.
+constexpr int kInstanceEntries = 4;
 // Postponing triangle tests (the wavefront's warp step modes) puts at most
 // one triangle group on the stack per wide level besides the node group, so
-// a BVH of depth d (TLAS + BLAS levels) with 2 d + 3 <= kStackSize never
+// a BVH of depth d (TLAS + BLAS levels) with 2 d + 4 <= kStackSize never
 // overflows; deeper BVHs are traversed without postponing.
-constexpr bool trav_postpone_fits(int depth) { return 2 * depth + 3 <= kStackSize; }
+constexpr bool trav_postpone_fits(int depth) { return 2 * depth + kInstanceEntries <= kStackSize; }
+// Without postponing, a ray pushes at most one node group per wide level
+// on its path, plus the instance entry's four when it enters an instance
+// from the TLAS.
+constexpr int trav_stack_need(int tlas_depth, int blas_depth, bool direct) {
+    return direct ? blas_depth : tlas_depth + blas_depth + kInstanceEntries;
+}
 
 // One job of a batch (pt_batch_render): the values the kernels take from
 // the job instead of from Params.  Jobs are ordered by path_base.
@@ -76,6 +85,9 @@ struct Params {
     float4* accum;
     unsigned long long* counters;  // [0] closest-hit queries, [1] shadow queries, [2] paths
     int* status;                   // PT_OK or a PT_ERR_* code set by the kernels
+    // traversal stack entries a ray may push (kStackSize; a lower bound is a
+    // failure-detection test's way to make the overflow status fire)
+    int stack_limit;
     // batches (pt_batch_render): the jobs, paths left per job and the
     // %globaltimer at which each job's last path finished ([num_jobs]: start)
     const BatchJob* jobs;

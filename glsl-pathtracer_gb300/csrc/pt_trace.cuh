@@ -38,20 +38,28 @@ struct TRay {
     uint32_t oct_inv;
 };
 
+// 1/d rounded to nearest (__frcp_rn), whatever -prec-div says: the slab
+// planes then sit where IEEE arithmetic puts them, as in the oracle's
+// AABBIntersect (invDir = 1.0 / r.direction).  Three per ray set-up.
 __device__ __forceinline__ float safe_rcp(float d) {
-    return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
+    return __frcp_rn(fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
 }
 
-__device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
+// The ray (o, d) with its reciprocal direction given.
+__device__ __forceinline__ TRay make_tray(V3 o, V3 d, float ix, float iy, float iz) {
     TRay r;
     r.o = o;
     r.d = d;
-    r.ix = safe_rcp(d.x);
-    r.iy = safe_rcp(d.y);
-    r.iz = safe_rcp(d.z);
-    const uint32_t oct = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
+    r.ix = ix;
+    r.iy = iy;
+    r.iz = iz;
+    const uint32_t oct = (ix < 0.0f ? 1u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 4u : 0u);
     r.oct_inv = 7u - oct;
     return r;
+}
+
+__device__ __forceinline__ TRay prep_ray(V3 o, V3 d) {
+    return make_tray(o, d, safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
 }
 
 
@@ -288,8 +296,11 @@ __device__ __forceinline__ void flag_status(int* status, int code) { atomicCAS(s
 
 // --------------------------------------------------------- state machine
 // Entering an instance pushes the TLAS position (node group, then pending
-// instances) and a sentinel; popping the sentinel leaves the BLAS.
+// instances), the world ray's reciprocal direction (x and y; z rides in the
+// sentinel's second word) and a sentinel; popping the sentinel leaves the
+// BLAS with the world ray restored without recomputing its reciprocals.
 constexpr uint32_t kBlasSentinel = 0xffffffffu;
+static_assert(kInstanceEntries == 4, "an instance entry pushes four stack entries");
 
 struct Trav {
     V3 wo, wd;         // the query ray (world space)
@@ -338,8 +349,14 @@ enum { TRAV_RUNNING = 0, TRAV_DONE = 1, TRAV_HIT = 2 };
 constexpr int kTrisPerStep = 3;
 constexpr int kNodesPerStep = 2;
 
+// A push beyond the stack bound drops the entry (the subtree or triangles
+// it holds are not traversed) and sets PT_ERR_STACK_OVERFLOW in the status
+// word, which the host reads after the launch; the traversal itself goes on
+// and ends.  Entries are dropped one at a time only where each stands alone
+// (a node group, a postponed triangle group); the four entries of an
+// instance entry go on the stack together or not at all.
 __device__ __forceinline__ void trav_push(const Params& P, uint2* stack, int& sp, uint2 e) {
-    if (sp < kStackSize) stack[sp++] = e;
+    if (sp < P.stack_limit) stack[sp++] = e;
     else flag_status(P.status, PT_ERR_STACK_OVERFLOW);
 }
 
@@ -422,19 +439,27 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 }
             }
         } else {
-            // enter an instance: park the TLAS position on the stack
+            // enter an instance: park the TLAS position on the stack -- all
+            // four entries, or none when they do not fit: the instance is
+            // then skipped and the overflow status set, so that every later
+            // pop still finds entries of its own level
             const int b = __ffs(s.pbits) - 1;
             s.pbits &= s.pbits - 1;
+            if (s.sp + kInstanceEntries > P.stack_limit) {
+                flag_status(P.status, PT_ERR_STACK_OVERFLOW);
+                return TRAV_RUNNING;
+            }
             const int4 ir = __ldg(P.insts + s.pbase + b);
-            trav_push(P, stack, s.sp, s.ng);
-            trav_push(P, stack, s.sp, make_uint2(s.pbase, s.pbits));
-            trav_push(P, stack, s.sp, make_uint2(kBlasSentinel, 0u));
+            stack[s.sp++] = s.ng;
+            stack[s.sp++] = make_uint2(s.pbase, s.pbits);
+            stack[s.sp++] = make_uint2(__float_as_uint(s.cur.ix), __float_as_uint(s.cur.iy));
+            stack[s.sp++] = make_uint2(kBlasSentinel, __float_as_uint(s.cur.iz));
             s.pbits = 0;
             s.ng = make_uint2(0, 0);
             s.cur_inst = ir.y;
             s.cur_mat = ir.z;
-            s.cur = ir.w ? prep_ray(s.wo, s.wd)
-                         : prep_ray(xform_point(P.xf, ir.y, s.wo, 1.0f), xform_point(P.xf, ir.y, s.wd, 0.0f));
+            // in the TLAS s.cur is the world ray: an untransformed instance keeps it
+            if (!ir.w) s.cur = prep_ray(xform_point(P.xf, ir.y, s.wo, 1.0f), xform_point(P.xf, ir.y, s.wd, 0.0f));
             s.next = ir.x;
         }
         return TRAV_RUNNING;
@@ -449,12 +474,14 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 if (s.sp == 0) return TRAV_DONE;
                 const uint2 e = stack[--s.sp];
                 if (!DIRECT && e.x == kBlasSentinel) {  // back to the TLAS
+                    const uint2 inv = stack[--s.sp];
                     const uint2 pend = stack[--s.sp];
                     s.ng = stack[--s.sp];
                     s.pbase = pend.x;
                     s.pbits = pend.y;
                     s.cur_inst = -1;
-                    s.cur = prep_ray(s.wo, s.wd);
+                    s.cur = make_tray(s.wo, s.wd, __uint_as_float(inv.x), __uint_as_float(inv.y),
+                                      __uint_as_float(e.y));
                     return TRAV_RUNNING;
                 }
                 if (e.y <= 0x00ffffffu) {  // a postponed triangle group

@@ -174,6 +174,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.pt_update_lights.argtypes = [P, _f, C.c_int32]
     lib.pt_render_adjoint.argtypes = [P, C.c_int32, C.c_int32, _f, _f]
     lib.pt_get_accum.argtypes = [P, _f]
+    lib.pt_set_accum.argtypes = [P, _f]
     lib.pt_snapshot_accum.argtypes = [P]
     lib.pt_get_output.argtypes = [P, C.c_int32, C.c_int32, _u8]
     lib.pt_trace_rays.argtypes = [P, C.POINTER(pt_ray), C.c_int32, C.POINTER(pt_hit)]
@@ -194,7 +195,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     for name in ("pt_create", "pt_create_gpu_bvh", "pt_update_transforms", "pt_gpu_build_ms", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
                  "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile",
                  "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
-                 "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output",
+                 "pt_render_tile_noalloc", "pt_render_passes", "pt_get_accum", "pt_set_accum", "pt_snapshot_accum",
+                 "pt_get_output",
                  "pt_trace_rays", "pt_trace_shadow", "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune",
                  "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
                  "pt_get_stage_stats", "pt_get_stats", "pt_batch_create", "pt_batch_render",
@@ -209,7 +211,8 @@ HEADER_SYMBOLS = [
     "pt_create", "pt_create_gpu_bvh", "pt_update_transforms", "pt_gpu_build_ms", "pt_destroy", "pt_set_stream", "pt_set_camera", "pt_set_options", "pt_set_integrator",
     "pt_update_instances", "pt_update_envmap", "pt_clear_accum", "pt_render_tile", "pt_render_tile_noalloc",
     "pt_update_materials", "pt_update_lights", "pt_render_adjoint",
-    "pt_render_passes", "pt_get_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays", "pt_trace_shadow",
+    "pt_render_passes", "pt_get_accum", "pt_set_accum", "pt_snapshot_accum", "pt_get_output", "pt_trace_rays",
+    "pt_trace_shadow",
     "pt_bsdf_eval", "pt_bsdf_sample", "pt_autotune", "pt_get_tuning", "pt_set_tuning", "pt_set_stage_timing",
     "pt_get_stage_stats", "pt_get_stats",
     "pt_batch_create", "pt_batch_render", "pt_batch_stats", "pt_batch_destroy",

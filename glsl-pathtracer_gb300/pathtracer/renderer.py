@@ -88,6 +88,12 @@ class GpuRenderer:
         self._ck(self.lib.pt_get_accum(self.ctx, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
 
+    def set_accum(self, acc: np.ndarray):
+        """Checkpoint resume: the accumulation from a pt_get_accum copy."""
+        a = np.ascontiguousarray(acc, np.float32)
+        assert a.shape == (self.height, self.width, 4)
+        self._ck(self.lib.pt_set_accum(self.ctx, a.ctypes.data_as(C.POINTER(C.c_float))))
+
     def snapshot(self):
         self._ck(self.lib.pt_snapshot_accum(self.ctx))
 

@@ -154,6 +154,36 @@ class SceneData:
                     options=self.options, camera=self.camera)
         np.savez_compressed(path, meta=np.frombuffer(json.dumps(meta).encode(), np.uint8), **arrays)
 
+    def save_flat(self, path: str):
+        """One binary file of the scene for C++ callers: "PTSCENE1", 12 int32
+        counts (nodes, top level index, triangles, vertices, instances,
+        materials, lights, envmap width and height, textures, texture width
+        and height), the envmap total as a float, pt_render_options,
+        pt_camera, then the arrays in the order of the counts (vertices and
+        normals both with the vertex count; envmap RGB then CDF)."""
+        import struct
+        o, c = self.render_options(), self.pt_camera()
+        ew, eh = (self.envmap_rgb.shape[1], self.envmap_rgb.shape[0]) if self.envmap_rgb is not None else (0, 0)
+        tex = self.texture_maps if self.texture_maps is not None and self.texture_maps.size else None
+        nt, th, tw = (tex.shape[0], tex.shape[1], tex.shape[2]) if tex is not None else (0, 0, 0)
+        counts = [self.bvh_nodes.shape[0], int(self.top_level_index), self.vert_indices.shape[0],
+                  self.vertices_uvx.shape[0], self.transforms.shape[0], self.materials.shape[0],
+                  self.lights.shape[0], ew, eh, nt, tw, th]
+        with open(path, "wb") as fh:
+            fh.write(b"PTSCENE1")
+            fh.write(struct.pack("<12i", *counts))
+            fh.write(struct.pack("<f", float(self.envmap_total_sum)))
+            fh.write(bytes(o))
+            fh.write(bytes(c))
+            for a in (self.bvh_nodes, self.vert_indices, self.vertices_uvx, self.normals_uvy, self.transforms,
+                      self.materials, self.lights):
+                fh.write(np.ascontiguousarray(a).tobytes())
+            if ew:
+                fh.write(np.ascontiguousarray(self.envmap_rgb, F).tobytes())
+                fh.write(np.ascontiguousarray(self.envmap_cdf, F).tobytes())
+            if tex is not None:
+                fh.write(np.ascontiguousarray(tex, np.uint8).tobytes())
+
     @staticmethod
     def load_npz(path: str) -> "SceneData":
         z = np.load(path)

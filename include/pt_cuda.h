@@ -44,7 +44,10 @@ extern "C" {
 #define PT_ERR_INVALID_ARG    1  /* null pointer, bad size, bad index in scene data */
 #define PT_ERR_CUDA           2  /* a CUDA runtime call failed */
 #define PT_ERR_OUT_OF_MEMORY  3  /* device allocation failed */
-#define PT_ERR_STACK_OVERFLOW 4  /* traversal stack limit hit (kernel status word) */
+#define PT_ERR_STACK_OVERFLOW 4  /* traversal stack limit hit (kernel status word): pt_create rejects
+                                  * BVHs deeper than the stack (PT_ERR_UNSUPPORTED), so only a
+                                  * bound lowered through PT_TRAVERSAL_STACK_LIMIT (a failure-
+                                  * detection test's setting, read at pt_create) reaches it */
 #define PT_ERR_UNSUPPORTED    5  /* scene feature the kernels do not implement */
 #define PT_ERR_TIMEOUT        6  /* a bounded device wait ran out */
 #define PT_ERR_QUEUE_OVERFLOW 7  /* wavefront queue capacity exceeded */
@@ -320,6 +323,15 @@ int pt_render_passes(pt_context* ctx, int32_t first_pass, int32_t num_passes);
 /* Read the float4 accumulation (sum of samples, alpha in .w) into host
  * memory: render_width*render_height*4 floats. */
 int pt_get_accum(pt_context* ctx, float* host_rgba);
+
+/* No counterpart in the reference (its accumulation lives in a GL texture):
+ * checkpoint / resume.  Overwrites the accumulation with
+ * render_width*render_height*4 floats from host memory, as pt_get_accum
+ * wrote them.  Samples are a function of the pixel, the pass index and the
+ * tile, so a context that resumes from passes 0..k-1 (pt_set_accum, then
+ * pt_render_passes(ctx, k, n)) ends with the accumulation that rendering
+ * passes 0..k+n-1 in one go gives, bit for bit. */
+int pt_set_accum(pt_context* ctx, const float* host_rgba);
 
 /* Replaces: the buffer flip at the end of a sample pass
  * (src/core/Renderer.cpp:756-760), after which GetOutputBuffer shows the

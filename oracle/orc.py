@@ -55,12 +55,12 @@ def render(scene, options, camera, first_pass=0, num_passes=1, use_double=False,
     W, H = options.render_width, options.render_height
     accum = np.zeros((H, W, 4), np.float32)
     sq = np.zeros((H, W, 3), np.float32) if with_sq else None
-    cnt = np.zeros(9, np.uint64)
+    cnt = np.zeros(10, np.uint64)
     d = scene.desc()
     rc = lib().orc_render(C.byref(d), C.byref(options), C.byref(camera), first_pass, num_passes, int(use_double),
                           row_start, row_step, nthreads, _p(accum), _p(sq), _p(cnt), int(cull))
     assert rc == 0
-    keys = ["closest", "shadow", "nodes", "tris", "overflow", "paths", "tri_hits", "nodes_any", "tris_any"]
+    keys = ["closest", "shadow", "nodes", "tris", "overflow", "paths", "tri_hits", "nodes_any", "tris_any", "inner"]
     return accum, sq, dict(zip(keys, [int(x) for x in cnt]))
 
 

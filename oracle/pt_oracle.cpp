@@ -21,10 +21,10 @@ template <class R> int render_impl(const pt_scene_desc* d, const pt_render_optio
     if (row_step < 1) row_step = 1;
     if (nthreads > 0) omp_set_num_threads(nthreads);
     uint64_t c_closest = 0, c_shadow = 0, c_nodes = 0, c_tris = 0, c_overflow = 0, c_paths = 0, c_hits = 0;
-    uint64_t c_nodes_any = 0, c_tris_any = 0;
+    uint64_t c_nodes_any = 0, c_tris_any = 0, c_inner = 0;
     std::vector<int> rows;
     for (int y = row_start; y < H; y += row_step) rows.push_back(y);
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : c_closest, c_shadow, c_nodes, c_tris, c_overflow, c_paths, c_hits, c_nodes_any, c_tris_any)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : c_closest, c_shadow, c_nodes, c_tris, c_overflow, c_paths, c_hits, c_nodes_any, c_tris_any, c_inner)
     for (int ri = 0; ri < (int)rows.size(); ++ri) {
         const int py = rows[ri];
         Counters cnt;
@@ -52,12 +52,12 @@ template <class R> int render_impl(const pt_scene_desc* d, const pt_render_optio
         }
         c_closest += cnt.closest; c_shadow += cnt.shadow; c_nodes += cnt.nodes; c_tris += cnt.tris;
         c_overflow += cnt.overflow; c_hits += cnt.tri_hits;
-        c_nodes_any += cnt.nodes_any; c_tris_any += cnt.tris_any;
+        c_nodes_any += cnt.nodes_any; c_tris_any += cnt.tris_any; c_inner += cnt.inner;
     }
     if (counters) {
         counters[0] = c_closest; counters[1] = c_shadow; counters[2] = c_nodes;
         counters[3] = c_tris; counters[4] = c_overflow; counters[5] = c_paths; counters[6] = c_hits;
-        counters[7] = c_nodes_any; counters[8] = c_tris_any;
+        counters[7] = c_nodes_any; counters[8] = c_tris_any; counters[9] = c_inner;
     }
     return 0;
 }

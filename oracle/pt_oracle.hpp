@@ -291,6 +291,7 @@ template <class R> struct Light { V3<R> position, emission, u, v; R radius, area
 struct Counters {
     uint64_t closest = 0, shadow = 0, nodes = 0, tris = 0, overflow = 0, tri_hits = 0;
     uint64_t nodes_any = 0, tris_any = 0;  // the part of nodes / tris done by any-hit queries
+    uint64_t inner = 0;                    // interior-node visits (two slab tests each) of all queries
     uint64_t truncated = 0;                // paths ended at PT_MAX_PATH_ITERATIONS
 };
 
@@ -459,6 +460,7 @@ template <class R> inline void TraverseClosest(const Scene<R>& s, const Ray<R>& 
             continue;
         } else {
             R l0, r0;
+            if (cnt) cnt->inner++;
             R leftHit = AABBIntersect(s.node_min(leftIndex), s.node_max(leftIndex), rTrans, &l0);
             R rightHit = AABBIntersect(s.node_min(rightIndex), s.node_max(rightIndex), rTrans, &r0);
             if (mode == 1) {  // cull children whose entry lies beyond the best hit
@@ -634,6 +636,7 @@ template <class R> inline bool AnyHit(const Scene<R>& s, const Ray<R>& r, R maxD
             continue;
         } else {
             R l0, r0;
+            cnt.inner++;
             R leftHit = AABBIntersect(s.node_min(leftIndex), s.node_max(leftIndex), rTrans, &l0);
             R rightHit = AABBIntersect(s.node_min(rightIndex), s.node_max(rightIndex), rTrans, &r0);
             if (s.cull) {  // boxes entered beyond maxDist cannot occlude

@@ -13,10 +13,24 @@ pass estimates; its central finite differences give
     differences with h = 2e-3 and 1e-3 (error O(h^4)).
 Steps are relative (h max(1, |theta|)) and divided by the step the float32
 scene records actually take.
-Tolerance: per parameter |g_gpu - g_ref| <= 1e-3 |g_ref| + 1e-3 max|g_ref|
-(FP32 accumulation of the GPU, and the rare path whose FP32 and FP64 forms
-take different discrete decisions), and the whole vector within 1e-3
-relative in the 2-norm.
+The 64 checked parameters are drawn uniformly at random from all of them
+(11 per material, 3 per light).  With a random dI of both signs, a
+parameter's gradient is the small remainder of a sum over every sample of
+terms of both signs, so its error floor is set by the size of that sum,
+not by the remainder: G_abs = the adjoint's gradient for |dI| (the same
+sum with every term counted positive; for the emissions exactly the sum of
+magnitudes).  Tolerance per parameter:
+  |g_gpu - g_ref| <= 1e-3 |g_ref| + 4 |FD(h) - FD(2h)| + 10 spread_gpu
+                     + ABS_FLOOR |G_abs|
+where FD(h) - FD(2h) is that parameter's own finite-difference error
+estimate, spread_gpu the spread of the GPU gradient over repeated runs
+(its FP32 accumulation, summed by atomics in a varying order), and
+ABS_FLOOR |G_abs| the FP32 path's agreement with the FP64 oracle sample by
+sample (shading arithmetic at GLSL precision, and the rare path whose FP32
+and FP64 forms take different discrete decisions) summed over the image;
+and the whole vector within 1e-3 relative in the 2-norm.  One more check
+runs at the benchmark size (1M-triangle icosphere, 512 x 512, 16 spp,
+depth 6) on four random parameters.
 """
 import numpy as np
 import pytest
@@ -24,6 +38,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 PASSES = 4
+ABS_FLOOR = 1e-4  # relative to the gradient of the sum of magnitudes (see above)
 
 
 @pytest.fixture(scope="module")
@@ -57,15 +72,32 @@ def central_difference(f, theta0, i, h):
     return (f(tp) - f(tm)) / step
 
 
-def choose_params(sd, g, count, seed):
-    """Parameters with gradients well above the noise floor: all 12 light
-    emissions and the largest-gradient material parameters, drawn at random."""
-    from pathtracer import diff
-    nm = sd.materials.shape[0] * len(diff.MATERIAL_OFFSETS)
-    rng = np.random.RandomState(seed)
-    mat_idx = np.argsort(-np.abs(g[:nm]))[: 3 * count]
-    pick = rng.choice(mat_idx, count - (len(g) - nm), replace=False)
-    return np.concatenate([np.sort(pick), np.arange(nm, len(g))])
+def choose_params(g, count, seed):
+    """`count` parameters drawn uniformly at random from all of them."""
+    return np.sort(np.random.RandomState(seed).choice(len(g), count, replace=False))
+
+
+def check_gradient(got, spread, g_abs, ref_fd, ref_2h, idx, rel=1e-3):
+    """The per-parameter and 2-norm bars against the FD gradient and the
+    Richardson-extrapolated FP64 reference."""
+    ref64 = (4.0 * ref_fd - ref_2h) / 3.0
+    fd_noise = np.abs(ref_fd - ref_2h)
+    for ref, name in ((ref_fd, "FD h=1e-3"), (ref64, "FP64 reference")):
+        err = np.abs(got - ref)
+        tol = rel * np.abs(ref) + 4.0 * fd_noise + 10.0 * spread + ABS_FLOOR * np.abs(g_abs)
+        print(f"{name}: largest error / |G_abs| {np.max(err / np.maximum(np.abs(g_abs), 1e-300)):.2e}, "
+              f"largest error / tolerance {np.max(err / np.maximum(tol, 1e-300)):.3f}")
+        worst = np.argsort(-(err / np.maximum(tol, 1e-300)))[:5]
+        assert np.all(err <= tol), (name, [(int(idx[k]), got[k], ref[k], tol[k]) for k in worst])
+        assert np.linalg.norm(got - ref) <= rel * np.linalg.norm(ref), name
+
+
+def gpu_gradient(r, first, passes, dI, runs=3):
+    """The adjoint's gradient, its spread over `runs` runs, and the gradient
+    for |dI| (every term of the sum counted positive)."""
+    gs = np.stack([r.render_adjoint(first, passes, dI).astype(np.float64) for _ in range(runs)])
+    g_abs = r.render_adjoint(first, passes, np.abs(dI)).astype(np.float64)
+    return gs.mean(0), gs.max(0) - gs.min(0), g_abs
 
 
 def test_adjoint_matches_fp64_finite_differences(setup, orc):
@@ -75,22 +107,47 @@ def test_adjoint_matches_fp64_finite_differences(setup, orc):
     dI = np.random.RandomState(7).normal(size=(H, W, 3)).astype(np.float32)
     r.clear()
     r.render_passes(0, PASSES)
-    g = r.render_adjoint(0, PASSES, dI).astype(np.float64)
+    g, spread, g_abs = gpu_gradient(r, 0, PASSES, dI)
     assert np.isfinite(g).all() and np.abs(g).max() > 0
     theta0 = diff.get_params(sd.materials, sd.lights)
-    idx = choose_params(sd, g, 64, 3)
+    idx = choose_params(g, 64, 3)
     J = lambda th: detached_J(orc, sd, th, dI)
     ref_fd = np.array([central_difference(J, theta0, i, 1e-3) for i in idx])
-    # FP64 reference: Richardson extrapolation of steps 2e-3 and 1e-3 (O(h^4))
     ref_2h = np.array([central_difference(J, theta0, i, 2e-3) for i in idx])
-    ref64 = (4.0 * ref_fd - ref_2h) / 3.0
-    got = g[idx]
-    for ref, name in ((ref_fd, "FD h=1e-3"), (ref64, "FP64 reference")):
-        err = np.abs(got - ref)
-        tol = 1e-3 * np.abs(ref) + 1e-3 * np.abs(ref).max()
-        worst = np.argsort(-(err / tol))[:5]
-        assert np.all(err <= tol), (name, [(int(idx[k]), got[k], ref[k]) for k in worst])
-        assert np.linalg.norm(got - ref) <= 1e-3 * np.linalg.norm(ref), name
+    print(f"\n64 random parameters: {int((np.abs(g[idx]) > 0).sum())} with a nonzero gradient, "
+          f"|g| from {np.abs(g[idx]).min():.3g} to {np.abs(g[idx]).max():.3g}")
+    check_gradient(g[idx], spread[idx], g_abs[idx], ref_fd, ref_2h, idx)
+
+
+def test_adjoint_at_the_benchmark_size(ptlib, orc):
+    """The differentiable-materials workload itself (1,048,820 triangles, 32
+    materials, 4 lights, 512 x 512, 16 spp, depth 6): four random
+    parameters -- two material, two light -- against FP64 central
+    differences of the oracle's detached estimator."""
+    from pathtracer import capi, diff, scenes
+    from pathtracer.renderer import GpuRenderer
+    sd = scenes.diff_scene(freq=229, width=512, height=512, max_depth=6)
+    passes = 16
+    dI = np.random.RandomState(9).normal(size=(512, 512, 3)).astype(np.float32)
+    with GpuRenderer(sd) as r:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        r.render_passes(0, passes)
+        g, spread, g_abs = gpu_gradient(r, 0, passes, dI, runs=2)
+    nm = sd.materials.shape[0] * len(diff.MATERIAL_OFFSETS)
+    rng = np.random.RandomState(11)
+    idx = np.concatenate([rng.choice(nm, 2, replace=False), nm + rng.choice(len(g) - nm, 2, replace=False)])
+    theta0 = diff.get_params(sd.materials, sd.lights)
+    import dataclasses
+
+    def J(th):
+        mats, lts = diff.set_params(sd.materials, sd.lights, th)
+        e = dataclasses.replace(sd, materials=mats, lights=lts)
+        img = orc.render_detached(sd, e, sd.render_options(), sd.pt_camera(), 0, passes, use_double=True)
+        return float(np.sum(dI.astype(np.float64) * img))
+    ref_fd = np.array([central_difference(J, theta0, i, 1e-3) for i in idx])
+    ref_2h = np.array([central_difference(J, theta0, i, 2e-3) for i in idx])
+    print("\nbenchmark size:", [(int(i), float(a), float(b)) for i, a, b in zip(idx, g[idx], ref_fd)])
+    check_gradient(g[idx], spread[idx], g_abs[idx], ref_fd, ref_2h, idx)
 
 
 def test_adjoint_reuses_the_forward_pass(setup):
@@ -155,10 +212,15 @@ def test_torch_autograd_l2_loss(setup, orc):
         im = orc.render_detached(sd, e, sd.render_options(), sd.pt_camera(), 0, PASSES, use_double=True)
         return float(np.mean((im - target) ** 2))
 
-    idx = choose_params(sd, g, 16, 5)
+    # the sum of magnitudes behind each gradient: the adjoint of |dLoss/dI|
+    dLdI = (2.0 / img.numel()) * (img.detach().numpy() - target)
+    g_abs = r.render_adjoint(0, PASSES, np.abs(dLdI).astype(np.float32)).astype(np.float64)
+    idx = choose_params(g, 16, 5)
     ref = np.array([central_difference(L, theta0, i, 1e-3) for i in idx])
+    ref_2h = np.array([central_difference(L, theta0, i, 2e-3) for i in idx])
     err = np.abs(g[idx] - ref)
-    assert np.all(err <= 2e-3 * np.abs(ref) + 2e-3 * np.abs(ref).max()), list(zip(idx, g[idx], ref))
+    tol = 2e-3 * np.abs(ref) + 4.0 * np.abs(ref - ref_2h) + ABS_FLOOR * np.abs(g_abs[idx])
+    assert np.all(err <= tol), list(zip(idx, g[idx], ref, tol))
     r.update_materials(sd.materials)
     r.update_lights(sd.lights)
 

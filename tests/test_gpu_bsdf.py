@@ -8,11 +8,25 @@ anywhere.  A record is assigned to the lobe with the largest FP64 pdf share
 (diffuse, dielectric reflection, metal, glass, clearcoat).
 
 Tolerances (FP32 device arithmetic against FP64, on values > 1e-3 where
-relative error is meaningful): per lobe, median relative error of f and pdf
-< 1e-5 and 99th percentile < 1e-3 -- the same bounds the FP32 oracle meets
-(test_oracle_golden.py).  Against the reference's own FP32 outputs
-(ref_bsdf.npz): median < 1e-6, 99.9th percentile < 1e-3 (CUDA's and glibc's
-pow/exp/log differ in the last bits).
+relative error is meaningful).  The reference's formulas lose precision in
+FP32 on some records whatever the hardware: the Fresnel term normalised by
+F0, cancellations at grazing angles.  The reference's own arithmetic in
+FP32 (the FP32 oracle, bit-exact to the reference's DisneyEval,
+test_oracle_golden.py) measures that loss per record: its rounding noise
+is the largest relative error against FP64 over the record and six copies
+of it with V, N and L moved by one ulp at random (other rounding patterns
+of the same, equally conditioned, evaluation).  So, per lobe:
+  * on every record whose FP32 rounding noise is at most REF_NOISE = 2e-6
+    (about 17 ulp), the device's f and pdf are within 1e-5 relative of
+    FP64;
+  * the excluded fraction is printed per lobe (measured with the oracle:
+    diffuse 0.3%, dielectric 3.3%, metal 1.3%, glass 9.9%, clearcoat
+    19.9%) and bounded;
+  * over all records the median is below 1e-6 and the 99th percentile
+    below 1e-4.
+Against the reference's own FP32 outputs (ref_bsdf.npz): median < 1e-6,
+99.9th percentile < 1e-3 (CUDA's and glibc's pow/exp/log differ in the last
+bits).
 """
 import ctypes as C
 import importlib.util
@@ -26,6 +40,8 @@ from conftest import golden
 pytestmark = pytest.mark.gpu
 
 LOBES = ["diffuse", "dielectric", "metal", "glass", "clearcoat"]
+REL_BAR = 1e-5     # device against FP64
+REF_NOISE = 2e-6   # records on which the reference's FP32 arithmetic is this exact are held to REL_BAR
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -73,10 +89,36 @@ def test_bsdf_eval_vs_reference_fp32(renderer, orc):
         assert np.array_equal(got[~np.isfinite(ref)], ref[~np.isfinite(ref)], equal_nan=True)
 
 
+def _rec_err(f, pdf, f64, p64):
+    """Per record: the larger relative error of f (channels > 1e-3) and pdf."""
+    ef = np.where(np.abs(f64) > 1e-3, np.abs(f.astype(np.float64) - f64) / np.maximum(np.abs(f64), 1e-300), 0.0)
+    ep = np.abs(pdf.astype(np.float64) - p64) / p64
+    return np.maximum(ef.max(1), ep), ef.max(1), ep
+
+
+def fp32_rounding_noise(orc, sp, V, N, L, f64, p64, copies=6, seed=0):
+    """Per record: the largest relative error of the reference's FP32
+    arithmetic against FP64, over the record and `copies` copies with V, N
+    and L moved by one ulp at random."""
+    f32, p32, _, _ = orc.bsdf_eval(sp, V, N, L, use_double=False)
+    noise, _, _ = _rec_err(f32, p32, f64, np.maximum(p64, 1e-300))
+    rng = np.random.RandomState(seed)
+
+    def nudge(x):
+        return (x * (1 + rng.choice([-1, 1], x.shape) * np.float32(2.0 ** -23))).astype(np.float32)
+    for _ in range(copies):
+        Vp, Np, Lp = nudge(V), nudge(N), nudge(L)
+        a, b, _, _ = orc.bsdf_eval(sp, Vp, Np, Lp, use_double=False)
+        c, d, _, _ = orc.bsdf_eval(sp, Vp, Np, Lp, use_double=True)
+        noise = np.maximum(noise, _rec_err(a, b, c, np.maximum(d, 1e-300))[0])
+    return noise
+
+
 def test_bsdf_eval_per_lobe_vs_fp64(renderer, orc):
     sp, V, N, L = bsdf_inputs(1_000_000, 11)
     f, pdf = gpu_eval(renderer, sp, V, N, L)
     f64, p64, _, lp64 = orc.bsdf_eval(sp, V, N, L, use_double=True)
+    noise = fp32_rounding_noise(orc, sp, V, N, L, f64, p64)
     share = lp64 / np.maximum(lp64.sum(1, keepdims=True), 1e-300)
     dom = np.argmax(share, 1)
     report = []
@@ -84,19 +126,19 @@ def test_bsdf_eval_per_lobe_vs_fp64(renderer, orc):
         sel = (dom == k) & (p64 > 1e-3)
         if sel.sum() < 100:
             continue
-        ep = rel_err(pdf[sel], p64[sel])
-        fs, fr = f[sel].ravel(), f64[sel].ravel()
-        okf = np.abs(fr) > 1e-3
-        ef = rel_err(fs[okf], fr[okf])
-        report.append((name, int(sel.sum()), np.median(ef), np.quantile(ef, 0.99), ef.max(), np.median(ep),
-                       np.quantile(ep, 0.99), ep.max()))
-    print("\nlobe        n        f: median      p99      max    pdf: median      p99      max")
+        e, ef, ep = _rec_err(f[sel], pdf[sel], f64[sel], p64[sel])
+        keep = noise[sel] <= REF_NOISE
+        report.append((name, int(sel.sum()), 1.0 - keep.mean(), np.median(ef), np.median(ep), e[keep].max(),
+                       np.quantile(e, 0.99), e.max()))
+    print("\nlobe         n    excluded   f median  pdf median  max kept      p99   max all")
     for row in report:
-        print("%-10s %7d   %10.2e %9.2e %9.2e   %10.2e %9.2e %9.2e" % row)
+        print("%-10s %7d   %8.4f  %9.2e  %9.2e  %9.2e %9.2e %9.2e" % row)
     assert len(report) == 5
-    for name, n, fmed, f99, _, pmed, p99, _ in report:
-        assert fmed < 1e-5 and pmed < 1e-5, (name, fmed, pmed)
-        assert f99 < 1e-3 and p99 < 1e-3, (name, f99, p99)
+    for name, n, excl, fmed, pmed, kept_max, p99, _ in report:
+        assert kept_max < REL_BAR, (name, kept_max)
+        assert fmed < 1e-6 and pmed < 1e-6, (name, fmed, pmed)
+        assert p99 < 1e-4, (name, p99)
+        assert excl < 0.25, (name, excl)
 
 
 def test_bsdf_sample_vs_oracle(renderer, orc):
@@ -115,9 +157,18 @@ def test_bsdf_sample_vs_oracle(renderer, orc):
     # differences that can flip a choice on a handful of records
     same_dir = np.all(np.abs(Lg - Lo) < 1e-4, axis=1)
     assert same_dir.mean() > 0.999, same_dir.mean()
-    # pdf = inf (a delta-like lobe at its peak) must agree as such
+    # pdf = inf (a delta-like lobe at its peak) must agree as such, except
+    # where it is an FP32 artefact of the reference's GTR1: its denominator
+    # 1 + (a^2 - 1) (N.H)^2 reaches 0 when the rounded N.H is 1 at the
+    # clearcoat peak, while the device's cancellation-free form, like FP64
+    # at the same direction, stays finite
     fin = np.isfinite(po)
-    assert np.array_equal(np.isfinite(pg[same_dir]), fin[same_dir])
-    ok = same_dir & fin & (po > 1e-3)
+    fin_g = np.isfinite(pg)
+    differ = same_dir & (fin_g != fin)
+    if differ.any():
+        _, p64, _, _ = orc.bsdf_eval(sp[differ], V[differ], N[differ], Lg[differ], use_double=True)
+        assert np.all(fin_g[differ] & ~fin[differ] & np.isfinite(p64)), (pg[differ], po[differ], p64)
+        assert differ.mean() < 1e-4, differ.mean()
+    ok = same_dir & fin & fin_g & (po > 1e-3)
     e = rel_err(pg[ok], po[ok])
     assert np.median(e) < 1e-5 and np.quantile(e, 0.99) < 1e-3, (np.median(e), np.quantile(e, 0.99))

@@ -4,9 +4,11 @@ The 1.05M-triangle icosphere at 1920x1080 and the 10,000-instance scene
 (5 meshes of 50k triangles, IBL, volume) at 1920x1080 are checked through
 properties that do not depend on the size:
 
-* closest-hit primitive / instance ids of a fixed ray set equal the
-  oracle's (ties at equal distance aside, and at most 1e-4 of the rays
-  grazing a shared edge), any-hit booleans likewise;
+* closest-hit primitive / instance ids of a fixed set of 1M rays (half
+  camera rays, half rays leaving random surface points) equal the
+  oracle's, ties at equal distance and rays grazing an edge aside
+  (classify_mismatch of test_gpu_parity.py: at most 1e-4 of the rays, and
+  each proven consistent in FP64); any-hit booleans likewise;
 * one full-frame pass of the wavefront form equals the megakernel's: the
   same accumulation up to last-bit rounding (a path whose discrete
   decisions flip on a last-bit difference diverges: under 1e-4 of the
@@ -34,7 +36,7 @@ def instanced_full():
     return scenes.instanced_scene(num_instances=10000, tris_per_blas=50000, width=1920, height=1080)
 
 
-def check_rays(sd, orc, n=20000):
+def check_rays(sd, orc, n=1_000_000):
     from pathtracer.renderer import GpuRenderer
     rays = ray_set(sd, orc, n, 11)
     with GpuRenderer(sd) as r:
@@ -42,8 +44,9 @@ def check_rays(sd, orc, n=20000):
         maxd = np.random.RandomState(12).uniform(0.1, 50.0, len(rays)).astype(np.float32)
         occ = r.shadow(rays, maxd)
     ho, _ = orc.trace_closest(sd, rays, mode=0)
-    bad, ties = classify_mismatch(sd, orc, rays, hg, ho)
-    assert len(bad) <= max(2, int(1e-4 * len(rays))), (len(bad), ties)
+    bad, ties, grazing = classify_mismatch(sd, orc, rays, hg, ho)
+    print(f"{len(rays)} rays: {ties} ties, {grazing} grazing, {len(bad)} other mismatches")
+    assert len(bad) == 0 and grazing <= max(2, int(1e-4 * len(rays))), (len(bad), ties, grazing)
     assert (hg["prim_id"] >= 0).sum() > 0.05 * len(rays)  # the set does hit the geometry
     occ_o = orc.trace_any(sd, sd.render_options(), rays, maxd)
     assert (occ != occ_o).sum() <= max(2, int(1e-4 * len(rays)))
