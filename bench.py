@@ -252,6 +252,52 @@ def run_reference(args, cfg, name):
     print(json.dumps(line))
 
 
+def config_bench(name, steps, warmup, flush, peak):
+    """Another workload of the survey on the same rules as the headline:
+    autotuned wavefront, L2 flushed before each timed step, device time with
+    CUDA events, then one stage-timed step for the dominant kernel's
+    roofline (its algorithmic bytes per query from the oracle's counts)."""
+    import torch
+    from pathtracer import capi
+    from pathtracer.renderer import GpuRenderer
+    cfg = CONFIGS[name]
+    sd = make_scene(name, cfg)
+    spp = cfg["spp"]
+    res = {"workload": cfg["desc"]}
+    with GpuRenderer(sd) as r:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        res["tuning"] = r.autotune(spp)
+        for k in range(warmup):
+            r.render_passes(k * spp, spp)
+        ms, rays = [], 0
+        for k in range(steps):
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize()
+            r.render_passes((warmup + k) * spp, spp)
+            st = r.stats()
+            if st["status"] != 0:
+                raise RuntimeError(f"{name}: kernel status {st['status']}")
+            ms.append(st["kernel_ms"])
+            rays += st["closest"] + st["shadow"]
+        r.set_stage_timing(True)
+        flush.fill_(0)
+        torch.cuda.synchronize()
+        r.render_passes((warmup + steps) * spp, spp)
+        st = r.stats()
+        stages = r.stage_stats()
+        r.set_stage_timing(False)
+    b_ray, work = bytes_per_ray(sd, sd.render_options(), sd.pt_camera())
+    ext_ms, ext_n = stages["extend"]
+    a = work["bytes_per_closest_ray"] * st["closest"] / (ext_ms / 1000.0) / 1e9
+    res.update({"value": rays / (sum(ms) / 1000.0) / 1e6, "unit": "Mrays/s", "steps": steps,
+                "ms_per_step": statistics.mean(ms), "rays_per_step": rays / steps,
+                "stages_ms": {k: v[0] for k, v in stages.items()},
+                "roofline": {"bound": "hbm", "kernel": "wf_extend", "achieved": a, "peak": peak, "unit": "GB/s",
+                             "frac": a / peak, "bytes_per_closest_ray": work["bytes_per_closest_ray"],
+                             "share_of_frame": ext_ms / max(sum(v[0] for v in stages.values()), 1e-9)}})
+    return res
+
+
 ADJOINT_WORKLOAD = ("differentiable materials: icosphere 1,048,820 tris split into 32 materials (11 Disney "
                     "parameters each) + 4 sphere lights (emission rgb), 512x512, 16 spp, depth 6")
 
@@ -435,6 +481,8 @@ def main():
                     help="extra steps timed per kernel with CUDA events (roofline of the dominant kernel)")
     ap.add_argument("--batch-steps", type=int, default=2,
                     help="steps of the 64-job batched workload (p50/p99 job latency, aggregate Mrays/s; 0: skip)")
+    ap.add_argument("--config-steps", type=int, default=3,
+                    help="timed steps of each other workload (Cornell C1, instanced C3) in the default run (0: skip)")
     ap.add_argument("--drop-in-steps", type=int, default=5,
                     help="timed steps of the C++ drop-in class on the same frame (0: skip)")
     ap.add_argument("--small", action="store_true", help="small scene (profiling / quick checks)")
@@ -572,6 +620,14 @@ def main():
     if args.adjoint_steps > 0 and rank == 0 and not args.small:
         adjoint = adjoint_bench(args.adjoint_steps, stream, flush)
 
+    others = None
+    if args.config_steps > 0 and rank == 0 and not args.small and args.config == "icosphere_1m":
+        r.set_stream(None)
+        peak, _ = measured_peaks()
+        others = {name: config_bench(name, args.config_steps, args.warmup, flush, peak)
+                  for name in ("cornell", "instanced")}
+        r.set_stream(stream.cuda_stream)
+
     batch = None
     if args.batch_steps > 0 and rank == 0 and not args.small:
         r.set_stream(None)
@@ -676,6 +732,8 @@ def main():
             line["compare"] = other
         if drop_in:
             line["e2e_drop_in"] = drop_in
+        if others:
+            line["other_configs"] = others
         if adjoint:
             line["adjoint"] = adjoint
         if batch:

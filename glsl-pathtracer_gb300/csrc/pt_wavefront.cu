@@ -155,6 +155,19 @@ __device__ __forceinline__ void job_params(Params& Pj, const BatchJob& J) {
     Pj.accum = J.accum;
     Pj.flags &= J.num_lights > 0 ? ~0u : ~(uint32_t)F_LIGHTS;
 }
+// The part of job_params a traversal stage needs when it starts a ray: the
+// BLAS entry and the job's lights (LightsClosest / LightsAny, trav_init).
+// A ray start costs a few hundred instructions, so loading the whole job
+// record there (camera, resolution, accumulation ...) is not free.
+__device__ __forceinline__ void job_trav_params(Params& Pj, const BatchJob& J) {
+    Pj.tlas_root = J.tlas_root;
+    Pj.direct = J.direct;
+    Pj.entry_inst = J.entry_inst;
+    Pj.entry_mat = J.entry_mat;
+    Pj.lights = Pj.lights + 4 * J.light_base;
+    Pj.num_lights = J.num_lights;
+    Pj.flags &= J.num_lights > 0 ? ~0u : ~(uint32_t)F_LIGHTS;
+}
 // the job of path i (jobs ordered by path_base)
 __device__ __forceinline__ int job_of_path(const Params& P, int i) {
     int lo = 0, hi = P.num_jobs - 1;
@@ -171,10 +184,19 @@ __device__ __forceinline__ uint64_t global_timer() {
     return t;
 }
 // a path of job j has finished: the last one stamps the job's completion
+// A path of job table entry j has ended.  The lanes of a warp that end paths
+// of the same job together share one atomic: the lowest of them subtracts
+// their count, and the subtraction that takes the job's count to zero stamps
+// the global timer.  (One atomic per path put every path of a job on a
+// single address, which the L2 serialises: millions per frame.)
 __device__ __forceinline__ void job_path_done(const Params& P, int j) {
     if (!P.jobs) return;
     const int id = P.jobs[j].id;
-    if (atomicSub(P.job_remaining + id, 1) == 1) P.job_done[id] = global_timer();
+    const unsigned same = __match_any_sync(__activemask(), id);
+    if ((int)(threadIdx.x & 31) == __ffs(same) - 1) {
+        const int n = __popc(same);
+        if (atomicSub(P.job_remaining + id, n) == n) P.job_done[id] = global_timer();
+    }
 }
 
 __global__ void wf_batch_stamp(unsigned long long* t) { *t = global_timer(); }
@@ -298,7 +320,7 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
                 const int4 misc = B.misc[ray];
                 if constexpr (BATCH) {
                     Params Pj = P;
-                    job_params(Pj, P.jobs[misc.w]);
+                    job_trav_params(Pj, P.jobs[misc.w]);
                     tl = LightsClosest(Pj, r, misc.x, hr);
                     trav_init(s, Pj, r.origin, r.direction, tl);
                 } else {
@@ -601,7 +623,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
                 bool occluded;
                 if constexpr (BATCH) {
                     Params Pj = P;
-                    job_params(Pj, P.jobs[B.misc[path].w]);
+                    job_trav_params(Pj, P.jobs[B.misc[path].w]);
                     occluded = LightsAny(Pj, r, d.w);
                     if (!occluded) trav_init(s, Pj, r.origin, r.direction, d.w);
                 } else {
