@@ -89,6 +89,7 @@ struct pt_context {
     DevBuf<WideTri> tris;
     DevBuf<InstRef> insts;
     DevBuf<InstXf> xf;
+    DevBuf<uint4> inst_bounds;  // root_may_hit's bounds per InstRef (empty: no culling)
     DevBuf<int32_t> vidx;
     DevBuf<float4> verts, norms, mats, lights, env;
     DevBuf<float> cdf;
@@ -132,6 +133,48 @@ struct pt_context {
 
 namespace {
 
+// The bounds root_may_hit (pt_trace.cuh) tests per InstRef: word 0 of the
+// BLAS root (internal-child mask cleared), then the smallest qlo and largest
+// qhi byte per axis over the root's non-empty slots (bvh8.h's layout).
+__global__ void k_inst_bounds(const WideNode* __restrict__ nodes, const InstRef* __restrict__ refs, int count,
+                              uint4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t* w = nodes[refs[i].blas_root].w;
+    uint32_t lo[3] = {255u, 255u, 255u}, hi[3] = {0u, 0u, 0u};
+    for (int slot = 0; slot < 8; ++slot) {
+        const int word = slot >> 2, sh = 8 * (slot & 3);
+        if (!((w[6 + word] >> sh) & 0xffu)) continue;  // meta 0: empty slot
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = min(lo[k], (w[8 + 2 * k + word] >> sh) & 0xffu);       // w2.xy, w2.zw, w3.xy
+            hi[k] = max(hi[k], (w[14 + 2 * k + word] >> sh) & 0xffu);      // w3.zw, w4.xy, w4.zw
+        }
+    }
+    out[2 * i] = make_uint4(w[0], w[1], w[2], w[3] & 0x00ffffffu);
+    out[2 * i + 1] = make_uint4(lo[0] | lo[1] << 8 | lo[2] << 16, hi[0] | hi[1] << 8 | hi[2] << 16, 0u, 0u);
+}
+
+bool instance_culling_enabled() {
+    const char* v = std::getenv("PT_INSTANCE_BOUNDS");
+    return !(v && v[0] == '0');
+}
+
+// (Re)computes the instance bounds of `count` InstRefs over `nodes`; left
+// empty when PT_INSTANCE_BOUNDS=0 (every instance entered, for comparison).
+cudaError_t make_inst_bounds(DevBuf<uint4>& out, const WideNode* nodes, const InstRef* refs, int count,
+                             cudaStream_t s) {
+    if (!instance_culling_enabled() || count <= 0) {
+        out.free();
+        return cudaSuccess;
+    }
+    if (out.n != 2 * (size_t)count) {
+        cudaError_t e = out.alloc(2 * (size_t)count);
+        if (e != cudaSuccess) return e;
+    }
+    k_inst_bounds<<<(count + 255) / 256, 256, 0, s>>>(nodes, refs, count, out.p);
+    return cudaGetLastError();
+}
+
 uint32_t option_flags(const pt_context* c) {
     const pt_render_options& o = c->opts;
     uint32_t f = c->scene_flags;
@@ -153,6 +196,7 @@ Params make_params(const pt_context* c) {
     p.tris = reinterpret_cast<const float4*>(c->tris.p);
     p.insts = reinterpret_cast<const int4*>(c->insts.p);
     p.xf = reinterpret_cast<const float4*>(c->xf.p);
+    p.inst_bounds = c->inst_bounds.p;
     p.tlas_root = c->bvh.tlas_root;
     if (c->direct) {
         p.tlas_root = c->entry.blas_root;
@@ -254,6 +298,7 @@ int upload_bvh(pt_context* c) {
     CK(c->nodes.upload(c->bvh.nodes, c->bvh.num_nodes, c->stream));
     CK(c->tris.upload(c->bvh.tris, c->bvh.num_tris, c->stream));
     CK(c->insts.upload(c->bvh.insts, c->bvh.num_inst_refs, c->stream));
+    CK(make_inst_bounds(c->inst_bounds, c->nodes.p, c->insts.p, c->bvh.num_inst_refs, c->stream));
     c->direct = c->bvh.num_inst_refs == 1 && c->bvh.insts[0].identity;
     if (c->direct) c->entry = c->bvh.insts[0];
     const int need = trav_stack_need(c->bvh.tlas_depth, c->bvh.blas_depth, c->direct);
@@ -433,6 +478,7 @@ int gpu_rebuild(pt_context* c, const float* transforms) {
     c->bvh.num_nodes = g.num_nodes;
     c->bvh.num_tris = g.num_tris;
     c->bvh.num_inst_refs = g.num_insts;
+    CK(make_inst_bounds(c->inst_bounds, c->nodes.p, c->insts.p, g.num_insts, c->stream));
     c->direct = false;
     if (g.num_insts == 1) {
         InstRef r;
@@ -594,6 +640,7 @@ struct pt_batch {
     DevBuf<WideTri> tris;
     DevBuf<InstRef> insts;
     DevBuf<InstXf> xf;
+    DevBuf<uint4> inst_bounds;
     DevBuf<int32_t> vidx;
     DevBuf<float4> verts, norms, mats, lights;
     DevBuf<BatchJob> job_table;
@@ -743,6 +790,7 @@ int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
             mat_off += c->num_materials;
             light_off += (int)(c->lights.n / 4);  // a job without lights holds one padding record
         }
+        if (e == cudaSuccess) e = make_inst_bounds(b->inst_bounds, b->nodes.p, b->insts.p, ref_off, b->stream);
         if (e != cudaSuccess) { rc = cuda_err(e, "batch index fix-up"); break; }
         if ((e = b->counters.alloc(4)) != cudaSuccess || (e = b->status.alloc(1)) != cudaSuccess ||
             (e = b->remaining.alloc(n)) != cudaSuccess || (e = b->done.alloc(n + 1)) != cudaSuccess) {
@@ -862,6 +910,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.tris = reinterpret_cast<const float4*>(b->tris.p);
     p.insts = reinterpret_cast<const int4*>(b->insts.p);
     p.xf = reinterpret_cast<const float4*>(b->xf.p);
+    p.inst_bounds = b->inst_bounds.p;
     p.vidx = b->vidx.p;
     p.verts = b->verts.p;
     p.norms = b->norms.p;
@@ -960,7 +1009,7 @@ int pt_batch_stats(pt_batch* b, pt_stats* s) {
 int pt_batch_destroy(pt_batch* b) {
     if (!b) return PT_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    b->nodes.free(); b->tris.free(); b->insts.free(); b->xf.free(); b->vidx.free(); b->verts.free();
+    b->nodes.free(); b->tris.free(); b->insts.free(); b->xf.free(); b->inst_bounds.free(); b->vidx.free(); b->verts.free();
     b->norms.free(); b->mats.free(); b->lights.free(); b->job_table.free(); b->remaining.free(); b->done.free();
     b->counters.free(); b->status.free();
     wavefront_free(b->wf);
@@ -981,7 +1030,7 @@ int pt_gpu_build_ms(pt_context* c, float* ms) {
 int pt_destroy(pt_context* c) {
     if (!c) return PT_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->vidx.free(); c->verts.free();
+    c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->inst_bounds.free(); c->vidx.free(); c->verts.free();
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
     c->tex.free();
     c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();

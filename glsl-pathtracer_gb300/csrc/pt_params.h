@@ -49,6 +49,7 @@ struct Params {
     const float4* tris;     // WideTri, 3 x float4
     const int4* insts;      // InstRef
     const float4* xf;       // InstXf, 10 x float4 per instance
+    const uint4* inst_bounds;  // 2 x uint4 per InstRef (root_may_hit); null: every instance is entered
     int tlas_root;
     // direct != 0: the scene is one untransformed instance, and traversal
     // starts in its BLAS (tlas_root is then the BLAS root) as instance

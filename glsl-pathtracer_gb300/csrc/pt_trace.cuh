@@ -125,25 +125,43 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
 // 2^-8 of a quantisation step).  Entry and exit distances are three-input
 // max / min (sm_100+).  PACKED computes the near and far planes of an axis
 // as one packed pair (the same values, fewer instructions, more registers).
+// The plane set-up of a node (its first word w0: origin, scale exponents)
+// for ray r: adj = scale / d and the near / far constants C per axis.
+struct NodeFrame {
+    float adjx, adjy, adjz, cnx, cfx, cny, cfy, cnz, cfz;
+};
+__device__ __forceinline__ NodeFrame node_frame(uint4 w0, const TRay& r) {
+    NodeFrame f;
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    f.adjx = sx * r.ix;
+    f.adjy = sy * r.iy;
+    f.adjz = sz * r.iz;
+    const float orgx = (__uint_as_float(w0.x) - r.o.x) * r.ix;
+    const float orgy = (__uint_as_float(w0.y) - r.o.y) * r.iy;
+    const float orgz = (__uint_as_float(w0.z) - r.o.z) * r.iz;
+    f.cnx = __fmaf_rd(-kQBias, f.adjx, orgx);
+    f.cfx = __fmaf_ru(-kQBias, f.adjx, orgx);
+    f.cny = __fmaf_rd(-kQBias, f.adjy, orgy);
+    f.cfy = __fmaf_ru(-kQBias, f.adjy, orgy);
+    f.cnz = __fmaf_rd(-kQBias, f.adjz, orgz);
+    f.cfz = __fmaf_ru(-kQBias, f.adjz, orgz);
+    return f;
+}
+
 template <bool PACKED = false>
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
                                                    float tmax, uint32_t& child_base, uint32_t& prim_base,
                                                    uint32_t& imask) {
     const uint4* n = nodes + (size_t)idx * 5;
     const uint4 w0 = __ldg(n), w1 = __ldg(n + 1), w2 = __ldg(n + 2), w3 = __ldg(n + 3), w4 = __ldg(n + 4);
-    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
-    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
-    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
     imask = w0.w >> 24;
     child_base = w1.x;
     prim_base = w1.y;
-    const float adjx = sx * r.ix, adjy = sy * r.iy, adjz = sz * r.iz;
-    const float orgx = (__uint_as_float(w0.x) - r.o.x) * r.ix;
-    const float orgy = (__uint_as_float(w0.y) - r.o.y) * r.iy;
-    const float orgz = (__uint_as_float(w0.z) - r.o.z) * r.iz;
-    const float cnx = __fmaf_rd(-kQBias, adjx, orgx), cfx = __fmaf_ru(-kQBias, adjx, orgx);
-    const float cny = __fmaf_rd(-kQBias, adjy, orgy), cfy = __fmaf_ru(-kQBias, adjy, orgy);
-    const float cnz = __fmaf_rd(-kQBias, adjz, orgz), cfz = __fmaf_ru(-kQBias, adjz, orgz);
+    const NodeFrame f = node_frame(w0, r);
+    const float adjx = f.adjx, adjy = f.adjy, adjz = f.adjz;
+    const float cnx = f.cnx, cfx = f.cfx, cny = f.cny, cfy = f.cfy, cnz = f.cnz, cfz = f.cfz;
     const uint32_t oct_inv4 = r.oct_inv * 0x01010101u;
     const bool nx = !(r.oct_inv & 1u), ny = !(r.oct_inv & 2u), nz = !(r.oct_inv & 4u);
     uint32_t hits = 0;
@@ -187,6 +205,34 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
         }
     }
     return hits;
+}
+
+// Instance bounds (Params::inst_bounds, two words per InstRef, made by
+// inst_bounds_kernel): the first word of the BLAS root node (origin and
+// scale exponents, the internal-child mask cleared) and the union of the
+// root's child boxes in the root's own grid -- x: the smallest qlo bytes
+// (x | y << 8 | z << 16), y: the largest qhi bytes.  An empty root has
+// qlo 255 and qhi 0, which no ray hits.
+//
+// Whether intersect_node on the BLAS root could accept any child.  The
+// union box is tested with the root's own frame (node_frame) and the same
+// FMA per plane: the FMA's rounding is monotonic in the plane byte, so the
+// union's near distances are at most, and its far distances at least, those
+// of every child, and every child the node test would accept makes this
+// test pass.  Skipping the instances it rejects changes no result.
+__device__ __forceinline__ bool root_may_hit(const uint4* __restrict__ bounds, int ref, const TRay& r, float tmax) {
+    const uint4 w0 = __ldg(bounds + 2 * ref), q = __ldg(bounds + 2 * ref + 1);
+    const NodeFrame f = node_frame(w0, r);
+    const bool nx = !(r.oct_inv & 1u), ny = !(r.oct_inv & 2u), nz = !(r.oct_inv & 4u);
+    const uint32_t near = __byte_perm(q.x, q.y, (nx ? 4u : 0u) | (ny ? 0x50u : 0x10u) | (nz ? 0x600u : 0x200u));
+    const uint32_t far = __byte_perm(q.x, q.y, (nx ? 0u : 4u) | (ny ? 0x10u : 0x50u) | (nz ? 0x200u : 0x600u));
+    const float tnx = fmaf(qbyte_biased(near, 0), f.adjx, f.cnx);
+    const float tfx = fmaf(qbyte_biased(far, 0), f.adjx, f.cfx);
+    const float tny = fmaf(qbyte_biased(near, 1), f.adjy, f.cny);
+    const float tfy = fmaf(qbyte_biased(far, 1), f.adjy, f.cfy);
+    const float tnz = fmaf(qbyte_biased(near, 2), f.adjz, f.cnz);
+    const float tfz = fmaf(qbyte_biased(far, 2), f.adjz, f.cfz);
+    return fmax3f(tnx, tny, fmaxf(tnz, 0.0f)) <= fmin3f(tfx, tfy, fminf(tfz, tmax));
 }
 
 // Triangle test of closest_hit.glsl:128-143 (accept when u, v, t and
@@ -439,17 +485,23 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                 }
             }
         } else {
-            // enter an instance: park the TLAS position on the stack -- all
-            // four entries, or none when they do not fit: the instance is
-            // then skipped and the overflow status set, so that every later
-            // pop still finds entries of its own level
+            // enter an instance whose BLAS root the ray may hit (the
+            // others would be entered and left without a hit: root_may_hit)
+            // and park the TLAS position on the stack -- all four entries,
+            // or none when they do not fit: the instance is then skipped and
+            // the overflow status set, so that every later pop still finds
+            // entries of its own level
             const int b = __ffs(s.pbits) - 1;
             s.pbits &= s.pbits - 1;
+            const int4 ir = __ldg(P.insts + s.pbase + b);
+            // in the TLAS s.cur is the world ray: an untransformed instance keeps it
+            const TRay obj =
+                ir.w ? s.cur : prep_ray(xform_point(P.xf, ir.y, s.wo, 1.0f), xform_point(P.xf, ir.y, s.wd, 0.0f));
+            if (P.inst_bounds && !root_may_hit(P.inst_bounds, s.pbase + b, obj, s.tmax)) return TRAV_RUNNING;
             if (s.sp + kInstanceEntries > P.stack_limit) {
                 flag_status(P.status, PT_ERR_STACK_OVERFLOW);
                 return TRAV_RUNNING;
             }
-            const int4 ir = __ldg(P.insts + s.pbase + b);
             stack[s.sp++] = s.ng;
             stack[s.sp++] = make_uint2(s.pbase, s.pbits);
             stack[s.sp++] = make_uint2(__float_as_uint(s.cur.ix), __float_as_uint(s.cur.iy));
@@ -458,8 +510,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
             s.ng = make_uint2(0, 0);
             s.cur_inst = ir.y;
             s.cur_mat = ir.z;
-            // in the TLAS s.cur is the world ray: an untransformed instance keeps it
-            if (!ir.w) s.cur = prep_ray(xform_point(P.xf, ir.y, s.wo, 1.0f), xform_point(P.xf, ir.y, s.wd, 0.0f));
+            s.cur = obj;
             s.next = ir.x;
         }
         return TRAV_RUNNING;

@@ -26,9 +26,8 @@ CU_SOURCES = ["pt_kernels.cu", "pt_wavefront.cu", "pt_capi.cu", "pt_bvh_gpu.cu"]
 # defines sqrt through inversesqrt), not the IEEE-rounded results.  The
 # shading stage takes a third less time.  Hits do not depend on it: the
 # triangle test and the ray-origin offsets use explicitly rounded
-# operations (__fdiv_rn, __fmul_rn, __fmaf_rn ...), which no flag changes;
-# the slab test's reciprocal ray direction may differ in its last bits,
-# which moves the tested box bounds by as little.
+# operations (__fdiv_rn, __fmul_rn, __fmaf_rn ...), which no flag changes,
+# and the slab test's reciprocal ray direction is __frcp_rn.
 _GLSL_PRECISION = ["-prec-div=false", "-prec-sqrt=false"]
 FILE_FLAGS = {"pt_kernels.cu": _GLSL_PRECISION, "pt_wavefront.cu": _GLSL_PRECISION}
 CPP_SOURCES = ["bvh8_build.cpp", "cuda_renderer.cpp"]

@@ -367,7 +367,13 @@ def cornell(width=256, height=256, max_depth=4, tile=None) -> SceneData:
 
 
 def icosphere_scene(freq=229, width=1920, height=1080, max_depth=8, seed=1, tile=None) -> SceneData:
-    """~1.05M-triangle geodesic icosphere (20 * freq^2 triangles; freq=229 gives
+    """The icosphere workload (icosphere_recipe) built into reference-layout arrays."""
+    return build_scene(**icosphere_recipe(freq, width, height, max_depth, seed, tile))
+
+
+def icosphere_recipe(freq=229, width=1920, height=1080, max_depth=8, seed=1, tile=None) -> dict:
+    """build_scene's arguments for a
+    ~1.05M-triangle geodesic icosphere (20 * freq^2 triangles; freq=229 gives
     1,048,820), radially displaced by 3-octave value noise (amplitude 0.05,
     seed `seed`), split into 16 meshes by icosahedron face (face % 16), one
     material each: baseColor U[0,1]^3, metallic U{0,1}, roughness U[0.05,1],
@@ -398,7 +404,7 @@ def icosphere_scene(freq=229, width=1920, height=1080, max_depth=8, seed=1, tile
     cam = camera((0.0, 0.0, 3.2), (0.0, 0.0, 0.0), 45.0)
     opts = dict(render_width=width, render_height=height, tile_width=tile or 256, tile_height=tile or 256,
                 max_depth=max_depth)
-    return build_scene(meshes, instances, mats, [light], cam, opts)
+    return dict(meshes=meshes, instances=instances, materials=mats, lights=[light], cam=cam, options=opts)
 
 
 def diff_scene(freq=229, width=512, height=512, max_depth=6, num_materials=32, seed=1, tile=None) -> SceneData:
@@ -457,7 +463,14 @@ def sky_envmap(width=2048, height=1024, sun_dir=(0.4, 0.7, 0.3), sun_radius_deg=
 
 def instanced_scene(num_instances=10000, tris_per_blas=50000, width=1920, height=1080, max_depth=8, seed=5,
                     env_size=(2048, 1024), tile=None) -> SceneData:
-    """Two-level instancing + IBL + volume: 5 BLAS meshes (displaced spheres
+    """The instanced workload (instanced_recipe) built into reference-layout arrays."""
+    return build_scene(**instanced_recipe(num_instances, tris_per_blas, width, height, max_depth, seed, env_size,
+                                          tile))
+
+
+def instanced_recipe(num_instances=10000, tris_per_blas=50000, width=1920, height=1080, max_depth=8, seed=5,
+                     env_size=(2048, 1024), tile=None) -> dict:
+    """build_scene's arguments for two-level instancing + IBL + volume: 5 BLAS meshes (displaced spheres
     and tori, ~tris_per_blas triangles each), num_instances instances with
     uniform random rotation, scale U[0.5, 2] and positions in a 200 x 200
     plane; a synthetic equirect sky with a sun disc; one homogeneous-volume
@@ -492,4 +505,4 @@ def instanced_scene(num_instances=10000, tris_per_blas=50000, width=1920, height
     cam = camera((0.0, 45.0, -150.0), (0.0, 0.0, 0.0), 60.0)
     opts = dict(render_width=width, render_height=height, tile_width=tile or 256, tile_height=tile or 256,
                 max_depth=max_depth, enable_envmap=1, enable_volume_mis=1)
-    return build_scene(meshes, instances, mats, [], cam, opts, envmap=env)
+    return dict(meshes=meshes, instances=instances, materials=mats, lights=[], cam=cam, options=opts, envmap=env)

@@ -19,11 +19,17 @@ Run in a container that has the reference source (path in REF below) after
                          by the reference shaders with that macro set
   ref_tonemap.npz        the reference's tonemap.glsl on one accumulation
                          with every tonemap / background combination
-Usage: python make_golden.py [textured | features]
+  ref_tree_counts.json   traversal work per ray on the reference's own BVH
+                         (its loader, RadeonRays SBVH and BvhTranslator) and
+                         on this project's builder, for the icosphere and
+                         instanced workloads at full size: the source of the
+                         algorithmic bytes per ray of the roofline
+Usage: python make_golden.py [textured | features | trees]
 """
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 import sys
 import tempfile
@@ -326,7 +332,86 @@ TONEMAP_CASES = {
 }
 
 
+# ------------------------------------------------- reference BVH work counts
+def _obj_text(mesh) -> str:
+    """A non-indexed mesh as OBJ text: one v / vn per corner, faces in
+    order (the reference loader keeps OBJ faces as corner triples,
+    Mesh.cpp:65-101).  %.9g round-trips float32."""
+    P, N = mesh.verts[:, :3], mesh.norms[:, :3]
+    out = ["v %.9g %.9g %.9g\n" % tuple(p) for p in P]
+    out += ["vn %.9g %.9g %.9g\n" % tuple(n) for n in N]
+    out += ["f %d//%d %d//%d %d//%d\n" % (3 * i + 1, 3 * i + 1, 3 * i + 2, 3 * i + 2, 3 * i + 3, 3 * i + 3)
+            for i in range(mesh.num_tris)]
+    return "".join(out)
+
+
+def reference_scene_dump(recipe: dict, td: str, name: str) -> SceneData:
+    """Write a recipe's meshes and instances as a .scene file (Loader.cpp's
+    mesh blocks, one per instance, the transform as a `matrix` line), run the
+    reference's loader, BVH build and flattening on it, and return the
+    result with this project's materials, lights, environment map, camera
+    and options (the reference loader prepends a default material, so its
+    ids are this project's plus one)."""
+    mats = recipe["materials"]
+    lines = ["renderer\n{\n resolution 64 64\n}\n"]
+    for k in range(len(mats)):
+        lines.append(f"material m{k}\n{{\n color 1 1 1\n}}\n")
+    for k, mesh in enumerate(recipe["meshes"]):
+        with open(os.path.join(td, f"{name}_{k}.obj"), "w") as fh:
+            fh.write(_obj_text(mesh))
+    for mesh_id, mat_id, xf in recipe["instances"]:
+        # Loader.cpp:409-414 reads `matrix` row by row into xform[col][row]
+        m = np.asarray(xf, np.float32).reshape(4, 4).T.ravel()
+        lines.append(f"mesh\n{{\n file {name}_{mesh_id}.obj\n material m{mat_id}\n matrix "
+                     + " ".join("%.9g" % v for v in m) + "\n}\n")
+    path = os.path.join(td, name + ".scene")
+    with open(path, "w") as fh:
+        fh.write("".join(lines))
+    orc.ref_dump_scene(path, os.path.join(td, name))
+    rd = load_ref_dump(os.path.join(td, name))
+    ours = scenes.build_scene(**recipe)
+    assert np.array_equal(rd.transforms, ours.transforms), "transforms differ"
+    assert rd.materials.shape[0] == len(mats) + 1
+    rd.materials = np.concatenate([rd.materials[:1], ours.materials])
+    rd.lights = ours.lights
+    rd.envmap_rgb, rd.envmap_cdf, rd.envmap_total_sum = ours.envmap_rgb, ours.envmap_cdf, ours.envmap_total_sum
+    rd.options, rd.camera = ours.options, ours.camera
+    return rd, ours
+
+
+# the row sample bench.py's roofline counts on (every 64th row, 2 passes)
+TREE_SAMPLE = dict(row_step=64, passes=2)
+TREE_WORKLOADS = {
+    "icosphere_1m": lambda: scenes.icosphere_recipe(),
+    "instanced": lambda: scenes.instanced_recipe(),
+}
+
+
+def tree_counts() -> dict:
+    """Oracle traversal counters (tmax-culled, as bench.py counts them) on
+    the reference's BVH and on this project's, same rays and paths."""
+    out = {"sample": TREE_SAMPLE}
+    for name, make in TREE_WORKLOADS.items():
+        recipe = make()
+        with tempfile.TemporaryDirectory() as td:
+            rd, ours = reference_scene_dump(recipe, td, name)
+        res = {}
+        for tree, sd in (("reference", rd), ("ours", ours)):
+            _, _, c = orc.render(sd, ours.render_options(), ours.pt_camera(), 0, TREE_SAMPLE["passes"],
+                                 row_step=TREE_SAMPLE["row_step"], cull=True)
+            c["binary_nodes"] = int(sd.bvh_nodes.shape[0])
+            res[tree] = c
+        out[name] = res
+        print(name, res)
+    with open(os.path.join(HERE, "ref_tree_counts.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    return out
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "trees":
+        tree_counts()
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "textured":
         print("textured golden written", textured_golden())
         return
@@ -380,6 +465,7 @@ def main():
                         **{f"{k}_{f}": v for k, r in res.items() for f, v in r.items()})
     out["textured"] = textured_golden()
     out["features"] = feature_goldens()
+    tree_counts()
     print("golden fixtures written", out)
 
 
