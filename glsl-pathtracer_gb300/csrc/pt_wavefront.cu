@@ -106,6 +106,46 @@ __device__ __forceinline__ void load_path(const WfView& B, int i, PathState& ps)
     ps.job = misc.w;
 }
 
+// A path as StartPath leaves it (tile.glsl:41-74): throughput 1, radiance
+// 0 and no medium are constants, so wf_generate stores only the ray, the
+// RNG state and misc, and the shade launches of the first round
+// (with_first_round) read only those.
+__device__ __forceinline__ void store_path_start(const WfView& B, int i, const PathState& ps) {
+    B.o[i] = make_float4(ps.r.origin.x, ps.r.origin.y, ps.r.origin.z, ps.alpha);
+    B.d[i] = make_float4(ps.r.direction.x, ps.r.direction.y, ps.r.direction.z, ps.scatterPdf);
+    B.rng[i] = make_uint4(ps.rng.x, ps.rng.y, ps.rng.z, ps.rng.w);
+    B.misc[i] = make_int4(ps.depth, ps.matID,
+                          (ps.inMedium ? 1 : 0) | (ps.surfaceScatter ? 2 : 0) | (ps.medium.type << 8), ps.job);
+}
+__device__ __forceinline__ void load_path_start(const WfView& B, int i, PathState& ps) {
+    const float4 o = B.o[i], d = B.d[i];
+    const uint4 g = B.rng[i];
+    const int4 misc = B.misc[i];
+    ps.r.origin = v3(o.x, o.y, o.z);
+    ps.alpha = o.w;
+    ps.r.direction = v3(d.x, d.y, d.z);
+    ps.scatterPdf = d.w;
+    ps.throughput = v3(1.0f);
+    ps.prevRough = 0.0f;
+    ps.radiance = v3(0.0f);
+    ps.medium.density = 0.0f;
+    ps.medium.color = v3(0.0f);
+    ps.medium.anisotropy = 0.0f;
+    ps.rng.x = g.x; ps.rng.y = g.y; ps.rng.z = g.z; ps.rng.w = g.w;
+    ps.depth = misc.x;
+    ps.matID = misc.y;
+    ps.inMedium = misc.z & 1;
+    ps.surfaceScatter = (misc.z >> 1) & 1;
+    ps.medium.type = misc.z >> 8;
+    ps.job = misc.w;
+}
+// Bit 2 of an extend or shade launch's `in`: the launch belongs to the first
+// round, whose paths are all as wf_generate stored them (the replay form's
+// resume launches of that round included: a suspended path's state stays as
+// it was), and whose queue 0 is the identity, so path k is queue entry k.
+constexpr int kFirstRound = 4;
+__host__ __device__ __forceinline__ int with_first_round(int in, bool first) { return in | (first ? kFirstRound : 0); }
+
 template <int MEDIUM = 1>
 __device__ __forceinline__ void store_path(const WfView& B, int i, const PathState& ps) {
     B.o[i] = make_float4(ps.r.origin.x, ps.r.origin.y, ps.r.origin.z, ps.alpha);
@@ -241,7 +281,7 @@ __global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfVie
             const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
             StartPath(P, px, py, FrameNumber(P, W, first_pass + k, px, py), ps);
         }
-        store_path(B, i, ps);
+        store_path_start(B, i, ps);
         B.q[0][i] = i;
         ++paths;
     }
@@ -288,6 +328,8 @@ __device__ __forceinline__ int refill_target(bool exhausted, int refill) { retur
 template <int MINB, bool PACKED, bool BATCH = false, bool DIRECT = false>
 __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int in, int refill, int min_tris) {
     uint2 stack[kStackSize];
+    const bool first = (in & kFirstRound) != 0;  // queue `in` is the identity (wf_generate)
+    in &= 1;
     const int n = B.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         B.counts[in ^ 1] = 0;  // the next queue and the shadow queue start empty
@@ -314,7 +356,7 @@ __global__ void __launch_bounds__(128, MINB) wf_extend(Params P, WfView B, int i
             const int k = fetch_work(B.counts + 4, n, ray < 0);
             exhausted = __any_sync(0xffffffffu, ray < 0 && k < 0);
             if (k >= 0) {
-                ray = B.q[in][k];
+                ray = first ? k : B.q[in][k];
                 const float4 o = B.o[ray], d = B.d[ray];
                 const Ray r{v3(o.x, o.y, o.z), v3(d.x, d.y, d.z)};
                 const int4 misc = B.misc[ray];
@@ -462,14 +504,15 @@ __device__ __forceinline__ void adj_flush(const AdjView& A, const float* sgrad) 
 }
 
 // REPLAY (VOL_MIS with alpha materials): transmittance queries suspend the
-// shade step instead of tracing inline; `in` + 2 shades the resume queue.
+// shade step instead of tracing inline; `in` | 2 shades the resume queue.
 template <int MEDIUM, bool ENV, bool INLINE, bool ADJ = false, int MINB = 1, bool REPLAY = false, bool BATCH = false>
 __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in, RenderWork W, AdjView A) {
     uint2 stack[INLINE && !REPLAY ? kStackSize : 1];
     extern __shared__ float sgrad[];
     float* acc = nullptr;
     if (ADJ) acc = adj_accumulator(A, sgrad);
-    const bool resume = REPLAY && in >= 2;
+    const bool first = (in & kFirstRound) != 0;
+    const bool resume = REPLAY && (in & 2);
     in &= 1;
     const int* queue = resume ? B.qr : B.q[in];
     const int n = resume ? B.counts[6] : B.counts[in];
@@ -480,9 +523,10 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
         bool cont = false, shadow = false;
         int i = 0;
         if (valid) {
-            i = queue[j];
+            i = first && !resume ? j : queue[j];
             PathState ps;
-            load_path<MEDIUM>(B, i, ps);
+            if (first) load_path_start(B, i, ps);
+            else load_path<MEDIUM>(B, i, ps);
             HitRecord hr;
             const float4 h0 = B.h0[i];
             const int4 h1 = B.h1[i];
@@ -1050,7 +1094,7 @@ static cudaError_t launch_tail(const Params& p, const WfView& v, int in, int rou
     return cudaGetLastError();
 }
 
-// The replay form (VOL_MIS with alpha materials): in + 2 shades the resume queue.
+// The replay form (VOL_MIS with alpha materials): in | 2 shades the resume queue.
 cudaError_t launch_shade_replay(const Params& p, const WfView& v, int in, int grid, int block, cudaStream_t s) {
     if (p.flags & F_ENVMAP) wf_shade<2, true, true, false, 1, true><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
     else wf_shade<2, false, true, false, 1, true><<<grid, block, 0, s>>>(p, v, in, RenderWork{}, AdjView{});
@@ -1352,13 +1396,14 @@ template <class F> static cudaError_t timed(StageTimer* timer, int kind, cudaStr
 constexpr int kExtraRounds = 4;
 
 static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s,
-                                  StageTimer* timer, int* nl) {
+                                  StageTimer* timer, int* nl, bool first) {
     cudaError_t e;
-    if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, in, t, s); })) != cudaSuccess) return e;
+    const int sin = with_first_round(in, first);  // the first round's launches read no queue
+    if ((e = timed(timer, STAGE_EXTEND, s, [&] { return launch_extend(p, v, sin, t, s); })) != cudaSuccess) return e;
     if (wavefront_needs_replay(p.flags)) {
         const int sites = std::max(1, ((p.flags & F_ENVMAP) ? 1 : 0) + ((p.flags & F_LIGHTS) ? 1 : 0));
         if ((e = timed(timer, STAGE_SHADE, s,
-                       [&] { return launch_shade_replay(p, v, in, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
+                       [&] { return launch_shade_replay(p, v, sin, t.shade_grid, t.shade_block, s); })) != cudaSuccess)
             return e;
         for (int k = 0; k < sites; ++k) {
             if ((e = timed(timer, STAGE_SHADOW, s, [&] {
@@ -1368,7 +1413,7 @@ static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, cons
                 return e;
             if ((e = timed(timer, STAGE_SHADE, s, [&] {
                      cudaError_t ee = cudaMemsetAsync(v.counts + 2, 0, 4 * sizeof(int), s);
-                     return ee != cudaSuccess ? ee : launch_shade_replay(p, v, in + 2, t.shade_grid, t.shade_block, s);
+                     return ee != cudaSuccess ? ee : launch_shade_replay(p, v, sin | 2, t.shade_grid, t.shade_block, s);
                  })) != cudaSuccess)
                 return e;
         }
@@ -1377,7 +1422,7 @@ static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, cons
     }
     if ((e = timed(timer, STAGE_SHADE, s,
                    [&] {
-                       return shade_dispatch(p, v, in, t.shade_grid, t.shade_block, s, t.shade_variant,
+                       return shade_dispatch(p, v, sin, t.shade_grid, t.shade_block, s, t.shade_variant,
                                              t.shade_grid_v);
                    })) != cudaSuccess)
         return e;
@@ -1406,7 +1451,7 @@ static cudaError_t enqueue_batch(const Params& p, const RenderWork& W, const Wav
     const bool may_linger = (p.flags & F_ALPHA_TEST) != 0;
     const int rounds = iterations + (may_linger ? kExtraRounds : 0);
     for (int it = 0; it < rounds; ++it)
-        if ((e = enqueue_bounce(p, v, it & 1, t, s, timer, nl)) != cudaSuccess) return e;
+        if ((e = enqueue_bounce(p, v, it & 1, t, s, timer, nl, it == 0)) != cudaSuccess) return e;
     if (may_linger) {
         if ((e = timed(timer, STAGE_SHADE, s, [&] { return launch_tail(p, v, rounds & 1, rounds, t.shade_grid, s); })) !=
             cudaSuccess)
@@ -1501,8 +1546,9 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
         const int in = it & 1;
-        if ((e = launch_extend(p, v, in, t, s)) != cudaSuccess) return e;
-        wf_shade<0, false, false, true><<<t.shade_grid, t.shade_block, smem, s>>>(p, v, in, W, A);
+        if ((e = launch_extend(p, v, with_first_round(in, it == 0), t, s)) != cudaSuccess) return e;
+        wf_shade<0, false, false, true><<<t.shade_grid, t.shade_block, smem, s>>>(p, v, with_first_round(in, it == 0),
+                                                                                  W, A);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if ((e = launch_shadow<true>(p, v, t, A, smem, s)) != cudaSuccess) return e;
     }
@@ -1534,8 +1580,9 @@ cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chun
         const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
         for (int it = 0; it <= ch.max_depth; ++it) {
             const int in = it & 1;
-            if ((e = launch_extend<true>(pc, v, in, t, s)) != cudaSuccess) return e;
-            if ((e = launch_shade_plain<true>(pc, v, in, t.shade_variant, g3, t.shade_block, s)) != cudaSuccess)
+            if ((e = launch_extend<true>(pc, v, with_first_round(in, it == 0), t, s)) != cudaSuccess) return e;
+            if ((e = launch_shade_plain<true>(pc, v, with_first_round(in, it == 0), t.shade_variant, g3, t.shade_block,
+                                              s)) != cudaSuccess)
                 return e;
             if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
         }
