@@ -149,12 +149,12 @@ class ClockSampler:
 # (bounce 0 of a 1-spp frame, 2,073,600 camera rays) / its rays.  Traffic
 # grows with the rays of a launch: path-state reads and writes, BVH misses
 # in L2.
-EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 79.8}
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 75.0}
 # Warp-level instructions executed per closest-hit query by wf_extend on the
 # same ncu capture (smsp__inst_executed.sum of the launch / its rays): the
 # numerator of the instruction-issue roofline (4 warp instructions per cycle
 # per SM).
-EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 228.0}
+EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 211.4}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):

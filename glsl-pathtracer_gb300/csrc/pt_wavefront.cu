@@ -253,6 +253,31 @@ __device__ __forceinline__ void push(int* queue, int* count, int value, bool pre
     if (pred) queue[base + __popc(mask & ((1u << lane) - 1))] = value;
 }
 
+// Order of a pass's paths over the pixels of a w x h rectangle: bands of
+// four rows, each cut into blocks of eight columns (the last band and the
+// last block of a band may be smaller), blocks in column order within a
+// band, pixels of a block in row order.  The 32 paths of a warp are then an
+// 8 x 4 block of pixels rather than a 32-pixel row segment: camera rays
+// that hit nearby surface points traverse the same nodes and shade nearby
+// data.  Slot s -> pixel (x, y) and its inverse.
+__host__ __device__ __forceinline__ void slot_pixel(int s, int w, int h, int& x, int& y) {
+    const int band = s / (4 * w);
+    const int r = s - band * 4 * w;
+    const int hb = h - 4 * band < 4 ? h - 4 * band : 4;
+    const int full = w >> 3;
+    const int c = r / (8 * hb);
+    const int q = r - c * 8 * hb;
+    const int wb = c < full ? 8 : w - 8 * full;
+    y = 4 * band + q / wb;
+    x = 8 * c + q % wb;
+}
+__host__ __device__ __forceinline__ int pixel_slot(int x, int y, int w, int h) {
+    const int band = y >> 2, hb = h - 4 * band < 4 ? h - 4 * band : 4;
+    const int c = x >> 3, full = w >> 3;
+    const int wb = c < full ? 8 : w - 8 * full;
+    return band * 4 * w + c * 8 * hb + (y - 4 * band) * wb + (x - 8 * c);
+}
+
 // BATCH (this kernel and the stage kernels below): the batch form
 // (pt_batch_render), compiled apart so that the single-scene kernels carry
 // none of the per-job code.
@@ -271,14 +296,18 @@ __global__ void __launch_bounds__(256) wf_generate(Params P, RenderWork W, WfVie
             job_params(Pj, J);
             const int li = i - J.path_base;
             const int pix = li % J.npix, k = li / J.npix;
-            const int px = pix % J.width, py = pix / J.width;
+            int px, py;
+            slot_pixel(pix, J.width, J.height, px, py);
             RenderWork Wj = W;
             Wj.tile_frame = -1;
             StartPath(Pj, px, py, FrameNumber(Pj, Wj, J.first_pass + k, px, py), ps);
             ps.job = j;
         } else {
             const int pix = i % npix, k = i / npix;
-            const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+            int px, py;
+            slot_pixel(pix, W.w, W.h, px, py);
+            px += W.x0;
+            py += W.y0;
             StartPath(P, px, py, FrameNumber(P, W, first_pass + k, px, py), ps);
         }
         store_path_start(B, i, ps);
@@ -549,8 +578,11 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 h.P = &P;
                 h.A = &A;
                 h.acc = acc;
-                const int npix = W.w * W.h, pix = i % npix;
-                const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
+                const int npix = W.w * W.h;
+                int px, py;
+                slot_pixel(i % npix, W.w, W.h, px, py);
+                px += W.x0;
+                py += W.y0;
                 const float* di = A.dimage + 3 * ((size_t)py * A.width + px);
                 h.dL = v3(di[0], di[1], di[2]) * A.inv_passes;
                 const float4 lt = B.rad[i];
@@ -1023,8 +1055,9 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit_replay(Params P, WfView
 __global__ void __launch_bounds__(256) wf_resolve(Params P, RenderWork W, WfView B, int npass) {
     const int npix = W.w * W.h;
     for (int pix = blockIdx.x * blockDim.x + threadIdx.x; pix < npix; pix += gridDim.x * blockDim.x) {
-        const int px = W.x0 + pix % W.w, py = W.y0 + pix / W.w;
-        float4* out = P.accum + (size_t)py * P.width + px;
+        int px, py;  // pix is the path slot of the pixel in every pass
+        slot_pixel(pix, W.w, W.h, px, py);
+        float4* out = P.accum + (size_t)(W.y0 + py) * P.width + W.x0 + px;
         float4 acc = *out;
         for (int k = 0; k < npass; ++k) {
             const float4 r = B.rad[(size_t)k * npix + pix];
@@ -1047,8 +1080,10 @@ __global__ void __launch_bounds__(256) wf_resolve_batch(Params P, WfView B, int 
             else hi = mid - 1;
         }
         const BatchJob& J = P.jobs[lo];
-        const int pix = g - J.pixel_base;
-        float4* out = J.accum + pix;
+        const int pix = g - J.pixel_base;  // the path slot of the pixel in every pass
+        int px, py;
+        slot_pixel(pix, J.width, J.height, px, py);
+        float4* out = J.accum + (size_t)py * J.width + px;
         float4 acc = *out;
         for (int k = 0; k < J.num_passes; ++k) {
             const float4 r = B.rad[(size_t)J.path_base + (size_t)k * J.npix + pix];
@@ -1658,3 +1693,8 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
 }
 
 }  // namespace ptgb
+
+// Host copies of the path order (tests: a bijection for any rectangle).
+extern "C" void ptgb_slot_pixel(int s, int w, int h, int* x, int* y) { ptgb::slot_pixel(s, w, h, *x, *y); }
+extern "C" int ptgb_pixel_slot(int x, int y, int w, int h) { return ptgb::pixel_slot(x, y, w, h); }
+

@@ -280,3 +280,33 @@ def test_wide_bvh_collapse_fills_nodes():
     assert blas.mean() > 5.0, blas.mean()
     assert (blas == 2).mean() < 0.2
     assert tris.shape[0] == 20 * 40 * 40
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (7, 3), (8, 4), (9, 5), (16, 9), (33, 17), (256, 256), (1920, 1080),
+                                 (1921, 1079)])
+def test_path_order_is_a_bijection_of_warp_blocks(w, h):
+    """The wavefront's order of a pass's paths over the pixels (wf_generate,
+    the resolve kernels): every slot maps to a distinct pixel of the w x h
+    rectangle, the inverse returns the slot, and a full warp of 32 slots in
+    a full block is an 8 x 4 block of pixels."""
+    from pathtracer import capi
+    lib = capi.load_library()
+    lib.ptgb_pixel_slot.restype = C.c_int
+    x, y = C.c_int(), C.c_int()
+    seen = np.zeros((h, w), bool)
+    n = w * h
+    step = max(1, n // 20000)
+    for s in sorted(set(range(0, n, step)) | {n - 1}):
+        lib.ptgb_slot_pixel(s, w, h, C.byref(x), C.byref(y))
+        assert 0 <= x.value < w and 0 <= y.value < h, (s, x.value, y.value)
+        assert not seen[y.value, x.value] or step > 1
+        seen[y.value, x.value] = True
+        assert lib.ptgb_pixel_slot(x.value, y.value, w, h) == s
+    if step == 1:
+        assert seen.all()
+    if w >= 8 and h >= 4:
+        px = []
+        for s in range(32):
+            lib.ptgb_slot_pixel(s, w, h, C.byref(x), C.byref(y))
+            px.append((x.value, y.value))
+        assert sorted(px) == sorted((i, j) for i in range(8) for j in range(4))
