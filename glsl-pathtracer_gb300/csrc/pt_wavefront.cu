@@ -828,7 +828,9 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit(Params P, WfView B, int
     // per-thread stage: 0 start env ray, 1 tracing it, 2 start light ray,
     // 3 tracing it, 4 both done
     int path = -1, bits = 0, stage = 0, seg = 0;
-    bool exhausted = false;
+    // seg_end: the lane's segment traversal ended and its hit is not yet
+    // evaluated (done with the warp's retire / refill, as in wf_transmit_replay)
+    bool exhausted = false, seg_end = false;
     V3 origin = v3(0.0f), T0 = v3(1.0f), T1 = v3(1.0f);
     Ray r;
     float tl = PT_INF;
@@ -891,6 +893,19 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit(Params P, WfView B, int
         }
     };
     for (;;) {
+        if (seg_end) {  // the surface the segment hit: go through it (next segment) or end the ray
+            seg_end = false;
+            HitRecord hr;
+            hr.isEmitter = light_hit;
+            FinishClosest(s, tl, hr);
+            V3 T = stage == 1 ? T0 : T1;
+            const int st = transmit_hit(P, hr, r, T);
+            if (st == 2) T = v3(0.0f);
+            if (stage == 1) T0 = T;
+            else T1 = T;
+            if (st == 1 && ++seg < P.max_depth) segment();  // through a refractive surface
+            else stage += 1;
+        }
         start();
         resolve();
         if (!exhausted) {
@@ -915,20 +930,8 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit(Params P, WfView B, int
         while (__popc(__ballot_sync(0xffffffffu, !busy)) < target) {
             const int mode = min_tris > 0 ? trav_warp_mode(s, busy, min_tris) : TRAV_LANE;
             if (busy && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING) {
-                HitRecord hr;
-                hr.isEmitter = light_hit;
-                FinishClosest(s, tl, hr);
-                V3 T = stage == 1 ? T0 : T1;
-                const int st = transmit_hit(P, hr, r, T);
-                if (st == 2) T = v3(0.0f);
-                if (stage == 1) T0 = T;
-                else T1 = T;
-                if (st == 1 && ++seg < P.max_depth) {
-                    segment();  // through a refractive surface: the next segment
-                } else {
-                    stage += 1;
-                    busy = false;
-                }
+                busy = false;
+                seg_end = true;
             }
         }
     }
@@ -985,7 +988,10 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit_replay(Params P, WfView
     Counters cnt{0, 0};
     Trav s;
     int path = -1, seg = 0, slot = 0;
-    bool exhausted = false, tracing = false;
+    // seg_end: the lane's segment traversal ended and its hit is not yet
+    // evaluated; the warp evaluates such hits together, with its retire /
+    // refill, rather than in the traversal loop where the other lanes wait
+    bool exhausted = false, tracing = false, seg_end = false;
     V3 T = v3(1.0f);
     Ray r;
     Rng rng{0u, 0u, 0u, 0u};
@@ -999,6 +1005,18 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit_replay(Params P, WfView
         trav_init(s, P, r.origin, r.direction, tl);
     };
     for (;;) {
+        if (seg_end) {  // the surface the segment hit: go through it (next segment) or stop
+            seg_end = false;
+            HitRecord hr;
+            hr.isEmitter = light_hit;
+            FinishClosest(s, tl, hr);
+            const int st = transmit_hit_rng(P, hr, r, T, rng);
+            if (st == 2) T = v3(0.0f);
+            if (st == 1 && ++seg < P.max_depth) {
+                segment();
+                tracing = true;
+            }
+        }
         // retire: record the finished queries, queue their paths again
         const bool fin = path >= 0 && !tracing;
         if (fin) {
@@ -1039,13 +1057,8 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit_replay(Params P, WfView
         do {
             const int mode = min_tris > 0 ? trav_warp_mode(s, tracing, min_tris) : TRAV_LANE;
             if (tracing && trav_step<false, false, PACKED>(s, P, stack, nullptr, mode) != TRAV_RUNNING) {
-                HitRecord hr;
-                hr.isEmitter = light_hit;
-                FinishClosest(s, tl, hr);
-                const int st = transmit_hit_rng(P, hr, r, T, rng);
-                if (st == 2) T = v3(0.0f);
-                if (st == 1 && ++seg < P.max_depth) segment();
-                else tracing = false;
+                tracing = false;
+                seg_end = true;
             }
         } while (__popc(__ballot_sync(0xffffffffu, !tracing)) < target);
     }
