@@ -114,17 +114,6 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
 #endif
 }
 
-// Slab test of the eight children of wide node `idx`; returns the hit mask.
-// A plane's distance is q * adj + org with q the plane's byte, adj =
-// scale / d and org = (node origin - o) / d.  It is evaluated as one FMA,
-// Q * adj + C, with Q = 2^15 + q (exact, qbyte_biased) and C = org - 2^15 *
-// adj rounded down for near planes and up for far planes.  Rounding is
-// monotonic, so a near distance is never above fl(q * adj + org) and a far
-// distance never below it: the test accepts every box that the two-step
-// form fl((Q - 2^15) * adj + org) accepts, and more only by ulp(C) (about
-// 2^-8 of a quantisation step).  Entry and exit distances are three-input
-// max / min (sm_100+).  PACKED computes the near and far planes of an axis
-// as one packed pair (the same values, fewer instructions, more registers).
 // The plane set-up of a node (its first word w0: origin, scale exponents)
 // for ray r: adj = scale / d and the near / far constants C per axis.
 struct NodeFrame {
@@ -150,6 +139,17 @@ __device__ __forceinline__ NodeFrame node_frame(uint4 w0, const TRay& r) {
     return f;
 }
 
+// Slab test of the eight children of wide node `idx`; returns the hit mask.
+// A plane's distance is q * adj + org with q the plane's byte, adj =
+// scale / d and org = (node origin - o) / d.  It is evaluated as one FMA,
+// Q * adj + C, with Q = 2^15 + q (exact, qbyte_biased) and C = org - 2^15 *
+// adj rounded down for near planes and up for far planes.  Rounding is
+// monotonic, so a near distance is never above fl(q * adj + org) and a far
+// distance never below it: the test accepts every box that the two-step
+// form fl((Q - 2^15) * adj + org) accepts, and more only by ulp(C) (about
+// 2^-8 of a quantisation step).  Entry and exit distances are three-input
+// max / min (sm_100+).  PACKED computes the near and far planes of an axis
+// as one packed pair (the same values, fewer instructions, more registers).
 template <bool PACKED = false>
 __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
                                                    float tmax, uint32_t& child_base, uint32_t& prim_base,
@@ -425,8 +425,8 @@ __device__ __forceinline__ bool trav_can_descend(const Trav& s) {
 
 // One step.  ANY: stop at the first accepted triangle (any-hit query);
 // ALPHA (with ANY): anyhit.glsl:118-141's alpha test, drawing from rng.
-// A step tests one triangle, enters one instance, or picks the nearest
-// internal child of the current node group -- popping the next group off
+// A step tests one triangle, enters one instance and visits its BLAS root,
+// or picks the nearest internal child of the current node group -- popping the next group off
 // the stack first when the current one is exhausted -- and intersects it.
 // Closest hits: the nearest triangle wins; of triangles at exactly the same
 // distance, the one of smallest (triangle, instance) id, so the result does
@@ -484,7 +484,9 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
                     }
                 }
             }
-        } else {
+            return TRAV_RUNNING;
+        }
+        {
             // enter an instance whose BLAS root the ray may hit (the
             // others would be entered and left without a hit: root_may_hit)
             // and park the TLAS position on the stack -- all four entries,
@@ -511,9 +513,8 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
             s.cur_inst = ir.y;
             s.cur_mat = ir.z;
             s.cur = obj;
-            s.next = ir.x;
+            s.next = ir.x;  // the BLAS root: visited below, in this step
         }
-        return TRAV_RUNNING;
     }
     // up to kNodesPerStep node visits: after a visit that leaves no triangles
     // pending, the step goes on into the nearest internal child
