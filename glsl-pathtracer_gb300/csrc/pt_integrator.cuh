@@ -465,7 +465,11 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
     sr.origin = scatterPos;
     if (ENV) {
         float lightPdf;
-        const V3 lightDir = SampleEnvMap(P, Li, lightPdf, rng);
+        V3 lightDir;
+        if (!hook.env_sample(Li, lightPdf, lightDir)) {
+            lightDir = SampleEnvMap(P, Li, lightPdf, rng);
+            hook.env_sampled(Li, lightPdf, lightDir);
+        }
         const Ray shadowRay{scatterPos, lightDir};
         if (volmis && INLINE) {
             V3 Tr;
@@ -623,6 +627,11 @@ struct NoHook {
         T = EvalTransmittance(P, r, rng, stack, cnt);
         return true;
     }
+    // DirectLight's environment sample: true if the hook supplies it (a
+    // re-run of a suspended step, whose query follows at once and restores
+    // the RNG state it left); env_sampled sees a sample just drawn
+    __device__ __forceinline__ bool env_sample(V3&, float&, V3&) { return false; }
+    __device__ __forceinline__ void env_sampled(V3, float, V3) {}
 };
 
 // One iteration of PathTrace's loop (pathtrace.glsl:301-473) for the hit in

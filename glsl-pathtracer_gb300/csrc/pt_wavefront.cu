@@ -59,11 +59,33 @@ __device__ __forceinline__ int replay_done(const WfView& B, int i) { return (B.m
 // already traced return their recorded transmittance and continue with the
 // RNG state they left; the next one suspends the step, keeping its ray and
 // the RNG state at that point for wf_transmit_replay.
+// A re-run also takes the environment sample of its first run (kept in sc0:
+// radiance and pdf, sd1: direction, when the step suspended at the
+// environment query) instead of drawing it again: the same values, without
+// the two dependent CDF searches.  The environment query is always the
+// step's first (DirectLight), so it is recorded whenever done > 0.
 struct ReplayHook : NoHook {
     const WfView* B;
     int i, done, site = 0;
     Ray ray;
     uint4 rng_at;
+    V3 env_Li, env_dir;
+    float env_pdf;
+    bool env_new = false;
+    __device__ __forceinline__ bool env_sample(V3& Li, float& pdf, V3& dir) {
+        if (done == 0) return false;
+        const float4 a = B->sc0[i], b = B->sd1[i];
+        Li = v3(a.x, a.y, a.z);
+        pdf = a.w;
+        dir = v3(b.x, b.y, b.z);
+        return true;
+    }
+    __device__ __forceinline__ void env_sampled(V3 Li, float pdf, V3 dir) {
+        env_Li = Li;
+        env_pdf = pdf;
+        env_dir = dir;
+        env_new = true;
+    }
     __device__ __forceinline__ bool transmit(const Params&, const Ray& r, Rng& rng, uint2*, Counters&, V3& T) {
         if (site < done) {
             const float4 t = site ? B->tr1[i] : B->tr0[i];
@@ -517,6 +539,8 @@ struct AdjHook {
         T = EvalTransmittance(P, r, rng, stack, cnt);
         return true;
     }
+    __device__ __forceinline__ bool env_sample(V3&, float&, V3&) { return false; }
+    __device__ __forceinline__ void env_sampled(V3, float, V3) {}
 };
 
 __device__ __forceinline__ float* adj_accumulator(const AdjView& A, float* sgrad) {
@@ -606,6 +630,10 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 if (sr.suspended) {  // the path is shaded again after its query is traced
                     B.so[i] = make_float4(rh.ray.origin.x, rh.ray.origin.y, rh.ray.origin.z, 0.0f);
                     B.sd0[i] = make_float4(rh.ray.direction.x, rh.ray.direction.y, rh.ray.direction.z, 0.0f);
+                    if (rh.env_new) {
+                        B.sc0[i] = make_float4(rh.env_Li.x, rh.env_Li.y, rh.env_Li.z, rh.env_pdf);
+                        B.sd1[i] = make_float4(rh.env_dir.x, rh.env_dir.y, rh.env_dir.z, 0.0f);
+                    }
                     if (rh.done) B.trng1[i] = rh.rng_at;
                     else B.trng0[i] = rh.rng_at;
                 }
