@@ -463,6 +463,37 @@ def drop_in_bench(sd, spp, steps, warmup):
             "path": "ptgb::CudaRenderer(GLSLPT::Scene*): RenderPasses + Update + GetOutputBuffer per step"}
 
 
+def batch_of_one_bench(steps):
+    """The largest job of the 64-job batch workload alone, `steps` frames
+    through its own pt_render_passes and then `steps` as a batch of one (the
+    batch kernels' per-job cost; profiling runs)."""
+    import torch
+    from pathtracer import build, capi
+    from pathtracer.renderer import GpuBatch, GpuRenderer
+    build.build_library()
+    jobs = batch_jobs(64)
+    big = max(range(len(jobs)), key=lambda j: jobs[j][0])
+    sd = _batch_scene((big, jobs[big]))
+    spp = jobs[big][2]
+    out = {"workload": "largest job of the batch workload alone", "job": {
+        "tris": 20 * jobs[big][0] ** 2, "resolution": jobs[big][1], "spp": spp, "depth": jobs[big][3]}}
+    with GpuRenderer(sd) as r:
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        ms = []
+        for k in range(steps):
+            r.render_passes(spp * k, spp)
+            ms.append(r.stats()["kernel_ms"])
+        out["render_passes_ms"] = ms
+        with GpuBatch([r]) as b:
+            ms = []
+            for k in range(steps):
+                b.render([spp * k], [spp])
+                ms.append(b.stats()["kernel_ms"])
+            out["batch_of_one_ms"] = ms
+    torch.cuda.synchronize()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -489,7 +520,11 @@ def main():
     ap.add_argument("--gpu-bvh", action="store_true",
                     help="build the BVH on the GPU (pt_create_gpu_bvh) instead of collapsing the host-built one")
     ap.add_argument("--spp", type=int, default=None, help="sample passes per step (profiling runs)")
+    ap.add_argument("--batch-of-one", action="store_true",
+                    help="only the largest batch job, alone and as a batch of one, --steps frames each (profiling)")
     args = ap.parse_args()
+    if args.batch_of_one:
+        return batch_of_one_bench(args.steps)
     cfg = dict(CONFIGS[args.config])
     if args.spp:
         cfg["spp"] = args.spp
