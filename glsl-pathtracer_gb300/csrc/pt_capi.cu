@@ -703,7 +703,10 @@ extern "C" {
 int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
     if (!jobs || n <= 0 || !out) return set_err(PT_ERR_INVALID_ARG, "invalid batch");
     *out = nullptr;
-    const uint32_t unsupported = F_MEDIUM | F_ALPHA_TEST | F_ENVMAP | F_TEXTURES | F_UNIFORM_LIGHT;
+    // each job keeps its own render options, environment map and texture
+    // maps; media and alpha-tested materials need the transmittance and
+    // inline any-hit stages, which batches do not run
+    const uint32_t unsupported = F_MEDIUM | F_ALPHA_TEST;
     uint32_t flags = 0;
     for (int j = 0; j < n; ++j) {
         pt_context* c = jobs[j];
@@ -711,16 +714,13 @@ int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
         if (c->device != jobs[0]->device) return set_err(PT_ERR_INVALID_ARG, "batch jobs must share a device");
         const uint32_t f = option_flags(c);
         if (f & unsupported)
-            return set_err(PT_ERR_UNSUPPORTED, "batches take surface scenes with analytic lights only (no media, "
-                                               "alpha test, environment map, texture maps or uniform light)");
-        const uint32_t g = f & ~(uint32_t)F_LIGHTS;
-        if (j == 0) flags = g;
-        else if (g != flags) return set_err(PT_ERR_UNSUPPORTED, "batch jobs must share their render options' flags");
+            return set_err(PT_ERR_UNSUPPORTED, "batches take surface scenes (no media, no alpha-tested materials)");
+        flags |= f;
     }
     pt_batch* b = new pt_batch;
     b->jobs.assign(jobs, jobs + n);
     b->device = jobs[0]->device;
-    b->flags = flags | F_LIGHTS;
+    b->flags = flags;  // the union: which kernel forms the batch needs
     int rc = PT_OK;
     do {
         cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
@@ -818,6 +818,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     const int n = (int)b->jobs.size();
     std::vector<BatchJob> base(n);
     std::vector<int> remaining(n);
+    uint32_t flags = 0;  // union of the jobs' flags
     std::vector<long> job_paths(n);
     long total = 0, max_npix = 0;
     for (int j = 0; j < n; ++j) {
@@ -852,6 +853,23 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         J.accum = c->accum.p;
         J.npix = J.width * J.height;
         J.id = j;
+        // the job's options now; the scene flags of its copy in the batch
+        // (pt_batch_create took no media and no alpha-tested materials)
+        J.flags = option_flags(c) & ~(uint32_t)(F_MEDIUM | F_ALPHA_TEST);
+        flags |= J.flags;
+        J.mollify_amt = o.roughness_mollification_amt;
+        for (int k = 0; k < 3; ++k) J.uniform_light[k] = o.uniform_light_col[k];
+        J.env = c->env.p;
+        J.cdf = c->cdf.p;
+        J.env_w = c->env_w;
+        J.env_h = c->env_h;
+        J.env_total = c->env_total;
+        J.env_intensity = o.envmap_intensity;
+        J.env_rot = o.envmap_rot / 360.0f;  // Renderer.cpp:778
+        J.tex = c->tex.p;
+        J.tex_w = c->tex_w;
+        J.tex_h = c->tex_h;
+        J.num_tex = c->num_tex;
         job_paths[j] = (long)J.npix * num_passes[j];
         if (job_paths[j] >= (1L << 31)) return set_err(PT_ERR_UNSUPPORTED, "pt_batch_render: job too large");
         remaining[j] = (int)job_paths[j];
@@ -917,8 +935,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.mats = b->mats.p;
     p.lights = b->lights.p;
     p.num_materials = (int)(b->mats.n / 8);
-    p.flags = b->flags;
-    p.mollify_amt = b->jobs[0]->opts.roughness_mollification_amt;
+    p.flags = flags;  // the kernel forms the jobs need; each path reads its job's own flags
     p.counters = b->counters.p;
     p.status = b->status.p;
     p.stack_limit = kStackSize;

@@ -463,7 +463,7 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
     sr.n = 0;
     sr.adds = 0;
     sr.origin = scatterPos;
-    if (ENV) {
+    if (ENV && (P.flags & F_ENVMAP)) {  // (a batch's job may have none)
         float lightPdf;
         V3 lightDir;
         if (!hook.env_sample(Li, lightPdf, lightDir)) {
@@ -650,7 +650,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
         if (!((F & F_HIDE_EMITTERS) && !(ps.depth > 0))) {
             if (F & F_UNIFORM_LIGHT) {
                 ps.radiance = ps.radiance + v3(P.uniform_light[0], P.uniform_light[1], P.uniform_light[2]) * ps.throughput;
-            } else if (ENV) {
+            } else if (ENV && (F & F_ENVMAP)) {  // (a batch's job may have none)
                 float envPdf;
                 V3 envCol = EvalEnvMap(P, ps.r, envPdf);
                 float misWeight = 1.0f;

@@ -41,6 +41,17 @@ struct BatchJob {
     int path_base, npix, num_passes, first_pass;
     int pixel_base;  // prefix of the jobs' pixel counts
     int id;          // the job's index in the batch (completion counters)
+    // the job's render options and its context's environment and texture
+    // maps (read in place, not copied into the batch)
+    uint32_t flags;
+    float mollify_amt;
+    float uniform_light[3];
+    const float4* env;
+    const float* cdf;
+    int env_w, env_h;
+    float env_total, env_intensity, env_rot;
+    const uchar4* tex;
+    int tex_w, tex_h, num_tex;
 };
 
 struct Params {

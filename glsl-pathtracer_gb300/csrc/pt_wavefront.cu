@@ -215,7 +215,20 @@ __device__ __forceinline__ void job_params(Params& Pj, const BatchJob& J) {
     Pj.cam_focal = J.cam_focal;
     Pj.cam_aperture = J.cam_aperture;
     Pj.accum = J.accum;
-    Pj.flags &= J.num_lights > 0 ? ~0u : ~(uint32_t)F_LIGHTS;
+    Pj.flags = J.flags;
+    Pj.mollify_amt = J.mollify_amt;
+    for (int k = 0; k < 3; ++k) Pj.uniform_light[k] = J.uniform_light[k];
+    Pj.env = J.env;
+    Pj.cdf = J.cdf;
+    Pj.env_w = J.env_w;
+    Pj.env_h = J.env_h;
+    Pj.env_total = J.env_total;
+    Pj.env_intensity = J.env_intensity;
+    Pj.env_rot = J.env_rot;
+    Pj.tex = J.tex;
+    Pj.tex_w = J.tex_w;
+    Pj.tex_h = J.tex_h;
+    Pj.num_tex = J.num_tex;
 }
 // The part of job_params a traversal stage needs when it starts a ray: the
 // BLAS entry and the job's lights (LightsClosest / LightsAny, trav_init).
@@ -228,7 +241,7 @@ __device__ __forceinline__ void job_trav_params(Params& Pj, const BatchJob& J) {
     Pj.entry_mat = J.entry_mat;
     Pj.lights = Pj.lights + 4 * J.light_base;
     Pj.num_lights = J.num_lights;
-    Pj.flags &= J.num_lights > 0 ? ~0u : ~(uint32_t)F_LIGHTS;
+    Pj.flags = J.flags;
 }
 // the job of path i (jobs ordered by path_base)
 __device__ __forceinline__ int job_of_path(const Params& P, int i) {
@@ -1179,15 +1192,15 @@ cudaError_t launch_shade_replay(const Params& p, const WfView& v, int in, int gr
 
 // The plain surface shade (no media, no environment map, deferred shadow
 // rays) in three register budgets: unbounded, 80 (6 blocks) and 64 (8).
-template <bool BATCH = false>
+template <bool BATCH = false, bool ENV = false>
 cudaError_t launch_shade_plain(const Params& p, const WfView& v, int in, int variant, const int grids[3], int block,
                                cudaStream_t s) {
     const RenderWork w{};
     const AdjView a{};
     switch (variant) {
-        case 1: wf_shade<0, false, false, false, 6, false, BATCH><<<grids[1], block, 0, s>>>(p, v, in, w, a); break;
-        case 2: wf_shade<0, false, false, false, 8, false, BATCH><<<grids[2], block, 0, s>>>(p, v, in, w, a); break;
-        default: wf_shade<0, false, false, false, 1, false, BATCH><<<grids[0], block, 0, s>>>(p, v, in, w, a); break;
+        case 1: wf_shade<0, ENV, false, false, 6, false, BATCH><<<grids[1], block, 0, s>>>(p, v, in, w, a); break;
+        case 2: wf_shade<0, ENV, false, false, 8, false, BATCH><<<grids[2], block, 0, s>>>(p, v, in, w, a); break;
+        default: wf_shade<0, ENV, false, false, 1, false, BATCH><<<grids[0], block, 0, s>>>(p, v, in, w, a); break;
     }
     return cudaGetLastError();
 }
@@ -1652,13 +1665,16 @@ cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chun
         const int gen_grid = std::min((ch.paths + 255) / 256, t.resident_blocks_256);
         wf_generate<true><<<gen_grid, 256, 0, s>>>(pc, RenderWork{}, v, 0, 0, ch.paths);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        // batches take surface scenes with analytic lights only: the plain shade
+        // batches take surface scenes (no media, no alpha test): the plain
+        // shade, with the environment-map code when a job has a map
         const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
+        const bool env = (p.flags & F_ENVMAP) != 0;
         for (int it = 0; it <= ch.max_depth; ++it) {
             const int in = it & 1;
             if ((e = launch_extend<true>(pc, v, with_first_round(in, it == 0), t, s)) != cudaSuccess) return e;
-            if ((e = launch_shade_plain<true>(pc, v, with_first_round(in, it == 0), t.shade_variant, g3, t.shade_block,
-                                              s)) != cudaSuccess)
+            const int sin = with_first_round(in, it == 0);
+            if ((e = env ? launch_shade_plain<true, true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)
+                         : launch_shade_plain<true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)) != cudaSuccess)
                 return e;
             if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
         }

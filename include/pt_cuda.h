@@ -204,14 +204,16 @@ int pt_gpu_build_ms(pt_context* ctx, float* ms);
  * pt_render_passes(job, first_pass[j], num_passes[j]) would add: the same
  * paths with the same random numbers, up to the last-bit rounding of the
  * batch kernels' separately compiled arithmetic.
- * Jobs share one device and their render options' feature flags, and carry
- * surface scenes with analytic lights only (PT_ERR_UNSUPPORTED otherwise:
- * no medium, alpha test, environment map, texture maps or uniform light).
- * The batch launches with the tuning (pt_autotune / pt_set_tuning) of the
- * first job that has one, else the default.  The contexts must outlive the
- * batch; scene, material and light updates made to a context after
- * pt_batch_create are not seen by the batch; camera and render-option
- * changes (same flags) are. */
+ * Jobs share one device.  Each keeps its own render options (Russian
+ * roulette, hidden emitters, background, uniform light, roughness
+ * mollification, normal-map convention ...), environment map and texture
+ * maps; scenes with a medium or alpha-tested materials are refused
+ * (PT_ERR_UNSUPPORTED).  The batch launches with the tuning (pt_autotune /
+ * pt_set_tuning) of the first job that has one, else the default.  The
+ * contexts must outlive the batch: environment and texture maps are read
+ * from them in place.  Scene, material and light updates made to a context
+ * after pt_batch_create are not seen by the batch; camera, render-option
+ * and environment-map changes are. */
 typedef struct pt_batch pt_batch;
 int pt_batch_create(pt_context* const* jobs, int32_t num_jobs, pt_batch** out_batch);
 /* job_ms (optional, num_jobs floats): per job, the time from the start of

@@ -8,16 +8,17 @@ on its own within the image tolerance of test_gpu_parity.py (the batch
 branch of the kernels reads the job's parameters and compiles to slightly
 different FP32 contractions, so last-bit differences occur, as between the
 wavefront and the megakernel).  Jobs differ in scene, resolution (ragged sizes included), depth,
-pass range and light count.
+pass range, light count, render options, environment map and texture maps.
 """
 import numpy as np
 import pytest
 
+from conftest import golden_scene
 from test_gpu_parity import image_agreement
 
 pytestmark = pytest.mark.gpu
 
-# render options whose feature flags a batch requires to agree across jobs
+# the render options of the jobs of the first tests
 COMMON = dict(enable_rr=1, rr_depth=2, enable_envmap=0, enable_uniform_light=0, hide_emitters=0,
               enable_background=0, transparent_background=0, enable_roughness_mollification=0,
               enable_volume_mis=0)
@@ -144,13 +145,65 @@ def test_single_job_batch(ptlib):
         assert frac >= 0.999 and mean_rel < 1e-4
 
 
+def opaque_textured():
+    """The textured golden scene (every texture slot) with all materials
+    made opaque: texture maps without the alpha test."""
+    sd = golden_scene("ref_scene_textured.npz")
+    sd.materials = sd.materials.copy()
+    sd.materials[:, 28] = 1.0  # opacity
+    sd.materials[:, 29] = 0.0  # alphaMode: opaque
+    return sd
+
+
+def test_batch_jobs_with_own_options_and_maps(ptlib):
+    """Jobs whose render options, environment maps and texture maps differ:
+    an environment map alone, the uniform light, hidden emitters over an
+    environment map, a distant light, roughness mollification, texture maps
+    (with a DirectX normal map) and a plain Cornell box with Russian
+    roulette off, in one batch; each equals its own render."""
+    from pathtracer import capi, scenes
+    from pathtracer.renderer import GpuBatch, GpuRenderer
+    tex = opaque_textured()
+    tex.options = dict(tex.options, opengl_normal_map=0)
+    jobs = [(golden_scene("feature_scene_env_only.npz"), 0, 3),
+            (golden_scene("feature_scene_uniform_light.npz"), 1, 2),
+            (golden_scene("feature_scene_hide_emitters.npz"), 0, 2),
+            (golden_scene("feature_scene_distant.npz"), 2, 3),
+            (golden_scene("feature_scene_mollification.npz"), 0, 2),
+            (tex, 0, 2),
+            (scenes.cornell(40, 24, max_depth=4), 3, 2)]
+    rs = [GpuRenderer(sd) for sd, _, _ in jobs]
+    rs[-1].set_options(capi.make_options(**dict(capi.options_dict(rs[-1].options), enable_rr=0)))
+    try:
+        ref = []
+        for r, (sd, fp, n) in zip(rs, jobs):
+            r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+            r.clear()
+            r.render_passes(fp, n)
+            ref.append(r.accum())
+            r.clear()
+        with GpuBatch(rs) as b:
+            b.render([fp for _, fp, _ in jobs], [n for _, _, n in jobs])
+            st = b.stats()
+        assert st["status"] == 0
+        assert st["paths"] == sum(r.width * r.height * n for r, (_, _, n) in zip(rs, jobs))
+        for k, (r, a) in enumerate(zip(rs, ref)):
+            got = r.accum()
+            frac, mean_rel = image_agreement(got, a)
+            assert frac >= 0.999 and mean_rel < 1e-4, (k, frac, mean_rel)
+            assert np.array_equal(got[..., 3], a[..., 3])
+    finally:
+        for r in rs:
+            r.close()
+
+
 def test_batch_rejects_unsupported_jobs(ptlib):
     from pathtracer import capi, scenes
     from pathtracer.renderer import GpuBatch, GpuRenderer
     a = GpuRenderer(scenes.cornell(16, 16), **COMMON)
     env = scenes.instanced_scene(num_instances=20, tris_per_blas=500, width=16, height=16, env_size=(32, 16))
-    b = GpuRenderer(env)
-    c = GpuRenderer(scenes.cornell(16, 16), **{**COMMON, "enable_rr": 0})
+    b = GpuRenderer(env)  # a medium
+    c = GpuRenderer(golden_scene("ref_scene_textured.npz"))  # alpha-tested materials
     try:
         for pair in ([a, b], [a, c]):
             with pytest.raises(capi.PTError) as e:
