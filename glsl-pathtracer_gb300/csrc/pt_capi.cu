@@ -397,7 +397,7 @@ int render(pt_context* c, const RenderWork& w) {
         const char* g = std::getenv("PT_WAVEFRONT_GRAPH");
         const bool use_graph = !(g && g[0] == '0');
         WavefrontTuning t = c->wf_tuning;
-        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = t.min_tris_first = t.min_tris_shadow_first = 0;
         c->timer.reset();
         c->fwd.valid = false;
         CK(launch_wavefront(p, w, c->wf, t, use_graph, c->stream, &c->launches,
@@ -951,7 +951,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     WavefrontTuning t = b->tuning;
     int depth = 0;
     for (pt_context* c : b->jobs) depth = std::max(depth, c->bvh.tlas_depth + c->bvh.blas_depth);
-    if (!trav_postpone_fits(depth)) t.min_tris = 0;
+    if (!trav_postpone_fits(depth)) t.min_tris = t.min_tris_first = t.min_tris_shadow_first = 0;
     int launches = 0;
     bool use_graph = b->use_graph;
     if (const char* e = std::getenv("PT_BATCH_GRAPH")) use_graph = std::atoi(e) != 0;
@@ -1205,7 +1205,7 @@ int pt_render_tile_noalloc(pt_context* c, int32_t tx, int32_t ty, int32_t frame)
         band.h = std::min(rows, w.h - y);
         int n = 0;
         WavefrontTuning t = c->wf_tuning;
-        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+        if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = t.min_tris_first = t.min_tris_shadow_first = 0;
         CK(launch_wavefront(p, band, wb, t, false, c->stream, &n));
         launches += n;
     }
@@ -1291,7 +1291,7 @@ int pt_render_adjoint(pt_context* c, int32_t first_pass, int32_t num_passes, con
                         c->fwd.w.tile_frame == w.tile_frame;
     if (int rc = begin_launch(c)) return rc;
     WavefrontTuning t = c->wf_tuning;
-    if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = 0;
+    if (!trav_postpone_fits(c->bvh.tlas_depth + c->bvh.blas_depth)) t.min_tris = t.min_tris_first = t.min_tris_shadow_first = 0;
     CK(launch_adjoint(make_params(c), w, c->wf, t, A, !cached, c->stream, &c->launches));
     if (int rc = end_launch(c)) return rc;
     c->fwd.valid = false;  // the replay leaves the forward state of the paths, but not in a reusable form
@@ -1447,6 +1447,10 @@ void tuning_out(const WavefrontTuning& t, float ms, pt_tuning* out) {
     out->min_tris = t.min_tris;
     out->shade_variant = t.shade_variant;
     out->frame_ms = ms;
+    out->extend_refill_first = t.extend_refill_first;
+    out->min_tris_first = t.min_tris_first;
+    out->shadow_refill_first = t.shadow_refill_first;
+    out->shadow_min_tris_first = t.min_tris_shadow_first;
 }
 }  // namespace
 
@@ -1493,7 +1497,7 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
         return PT_OK;
     };
     WavefrontTuning best = c->wf_tuning;
-    if (!postpone) best.min_tris = 0;
+    if (!postpone) best.min_tris = best.min_tris_first = best.min_tris_shadow_first = 0;
     float ms[STAGE_COUNT];
     do {
         // 1. kernel variants, extend and shadow chosen separately
@@ -1551,6 +1555,31 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
             if (rc) break;
             best.shade_variant = vsh;
         }
+        // 5. the first round on its own (camera rays, coherent per warp, and
+        // the shadow rays of their hits): refill threshold and quorum
+        if (postpone) {
+            const int rf[] = {20, 24, 28, 32};
+            const int mf[] = {2, 4, 6};
+            float be1 = 1e30f, bs1 = 1e30f;
+            int re1 = 0, me1 = -1, rs1 = 0, ms1 = -1;
+            for (int r : rf) {
+                for (int m : mf) {
+                    WavefrontTuning t = best;
+                    t.extend_refill_first = t.shadow_refill_first = r;
+                    t.min_tris_first = t.min_tris_shadow_first = m;
+                    if ((rc = measure(t, ms))) break;
+                    if (ms[STAGE_EXTEND] < be1) { be1 = ms[STAGE_EXTEND]; re1 = r; me1 = m; }
+                    if (ms[STAGE_SHADOW] < bs1) { bs1 = ms[STAGE_SHADOW]; rs1 = r; ms1 = m; }
+                }
+                if (rc) break;
+            }
+            if (rc) break;
+            // against the other rounds' own setting
+            WavefrontTuning t = best;
+            if ((rc = measure(t, ms))) break;
+            if (be1 < ms[STAGE_EXTEND]) { best.extend_refill_first = re1; best.min_tris_first = me1; }
+            if (bs1 < ms[STAGE_SHADOW]) { best.shadow_refill_first = rs1; best.min_tris_shadow_first = ms1; }
+        }
         if ((rc = measure(best, ms))) break;
     } while (false);
     timer.release();
@@ -1579,7 +1608,10 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
     if (!c || !in) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
     if (in->extend_variant < 0 || in->extend_variant > 3 || in->shadow_variant < 0 || in->shadow_variant > 3 ||
         in->extend_refill < 1 || in->extend_refill > 32 || in->shadow_refill < 1 || in->shadow_refill > 32 ||
-        in->min_tris < 0 || in->min_tris > 32 || in->shade_variant < 0 || in->shade_variant > 2)
+        in->min_tris < 0 || in->min_tris > 32 || in->shade_variant < 0 || in->shade_variant > 2 ||
+        in->extend_refill_first < 0 || in->extend_refill_first > 32 || in->shadow_refill_first < 0 ||
+        in->shadow_refill_first > 32 || in->min_tris_first < -1 || in->min_tris_first > 32 ||
+        in->shadow_min_tris_first < -1 || in->shadow_min_tris_first > 32)
         return set_err(PT_ERR_INVALID_ARG, "tuning value out of range");
     if (!c->wf_tuned) {
         CK(wavefront_default_tuning(c->wf_tuning, 128));
@@ -1591,6 +1623,10 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
     c->wf_tuning.shadow_refill = in->shadow_refill;
     c->wf_tuning.min_tris = in->min_tris;
     c->wf_tuning.shade_variant = in->shade_variant;
+    c->wf_tuning.extend_refill_first = in->extend_refill_first;
+    c->wf_tuning.min_tris_first = in->min_tris_first;
+    c->wf_tuning.shadow_refill_first = in->shadow_refill_first;
+    c->wf_tuning.min_tris_shadow_first = in->shadow_min_tris_first;
     return PT_OK;
 }
 

@@ -1378,7 +1378,12 @@ static cudaError_t launch_transmit_replay(const Params& p, const WfView& v, cons
 template <bool BATCH = false>
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
     const int g = t.extend_grid_v[t.extend_variant];
-    const int b = t.extend_block, r = t.extend_refill, m = t.min_tris;
+    // the first round's camera rays (coherent 8 x 4 blocks) may take their own
+    // refill threshold and triangle-step quorum
+    const bool first = (in & kFirstRound) != 0;
+    const int b = t.extend_block;
+    const int r = first && t.extend_refill_first > 0 ? t.extend_refill_first : t.extend_refill;
+    const int m = first && t.min_tris_first >= 0 ? t.min_tris_first : t.min_tris;
     // a batch takes the direct form when every job enters directly (p.direct)
     if (p.direct) {
         switch (t.extend_variant) {
@@ -1400,8 +1405,12 @@ static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const
 
 template <bool ADJ, bool BATCH = false>
 static cudaError_t launch_shadow(const Params& p, const WfView& v, const WavefrontTuning& t, const AdjView& A,
-                                 size_t smem, cudaStream_t s) {
-    const int b = t.shadow_block, r = t.shadow_refill, m = t.min_tris;
+                                 size_t smem, cudaStream_t s, bool first = false) {
+    // the first round's shadow rays (from the camera rays' hits) may take
+    // their own refill threshold and triangle-step quorum
+    const int b = t.shadow_block;
+    const int r = first && t.shadow_refill_first > 0 ? t.shadow_refill_first : t.shadow_refill;
+    const int m = first && t.min_tris_shadow_first >= 0 ? t.min_tris_shadow_first : t.min_tris;
     if (!ADJ && transmit_deferred(p.flags)) {
         const int g = t.transmit_grid_v[t.shadow_variant];
         switch (t.shadow_variant) {
@@ -1515,7 +1524,7 @@ static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, cons
                                              t.shade_grid_v);
                    })) != cudaSuccess)
         return e;
-    if ((e = timed(timer, STAGE_SHADOW, s, [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s); })) !=
+    if ((e = timed(timer, STAGE_SHADOW, s, [&] { return launch_shadow<false>(p, v, t, AdjView{}, 0, s, first); })) !=
         cudaSuccess)
         return e;
     *nl += 3;
@@ -1639,7 +1648,7 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
         wf_shade<0, false, false, true><<<t.shade_grid, t.shade_block, smem, s>>>(p, v, with_first_round(in, it == 0),
                                                                                   W, A);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if ((e = launch_shadow<true>(p, v, t, A, smem, s)) != cudaSuccess) return e;
+        if ((e = launch_shadow<true>(p, v, t, A, smem, s, it == 0)) != cudaSuccess) return e;
     }
     nl += 1 + 3 * iterations;
     return cudaSuccess;
@@ -1676,7 +1685,7 @@ cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chun
             if ((e = env ? launch_shade_plain<true, true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)
                          : launch_shade_plain<true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)) != cudaSuccess)
                 return e;
-            if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s)) != cudaSuccess) return e;
+            if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s, it == 0)) != cudaSuccess) return e;
         }
         const int res_grid = std::min((ch.pixels + 255) / 256, t.resident_blocks_256);
         wf_resolve_batch<<<res_grid, 256, 0, s>>>(pc, v, ch.pixels);
@@ -1741,6 +1750,22 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     if (const char* r = std::getenv("PT_WAVEFRONT_VARIANT")) {
         const int v = std::atoi(r);
         if (v >= 0 && v < 4) t.extend_variant = t.shadow_variant = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_REFILL_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 1 && v <= 32) t.extend_refill_first = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_MIN_TRIS_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v <= 32) t.min_tris_first = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_SHADOW_REFILL_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 1 && v <= 32) t.shadow_refill_first = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_SHADOW_MIN_TRIS_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v <= 32) t.min_tris_shadow_first = v;
     }
     if (const char* r = std::getenv("PT_WAVEFRONT_SHADE_VARIANT")) {
         const int v = std::atoi(r);

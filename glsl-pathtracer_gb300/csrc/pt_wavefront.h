@@ -42,6 +42,12 @@ struct WavefrontTuning {
     // triangles pending; fewer are postponed (0: every lane steps on its own;
     // PT_WAVEFRONT_MIN_TRIS overrides).  Needs trav_postpone_fits(depth).
     int min_tris = 8;
+    // the same two for the first round (camera rays and the shadow rays of
+    // their hits), per stage; <= 0 (refill) / < 0 (min_tris): as the other
+    // rounds (PT_WAVEFRONT_REFILL_FIRST, PT_WAVEFRONT_MIN_TRIS_FIRST,
+    // PT_WAVEFRONT_SHADOW_REFILL_FIRST, PT_WAVEFRONT_SHADOW_MIN_TRIS_FIRST)
+    int extend_refill_first = 0, min_tris_first = -1;
+    int shadow_refill_first = 0, min_tris_shadow_first = -1;
     int extend_grid = 0, shade_grid = 0, shadow_grid = 0;
     // kernel variants of the traversal stages: 0 = 8 blocks (64 registers),
     // scalar node test; 1 = 8 blocks, packed; 2 = 6 blocks (80 registers),

@@ -383,6 +383,14 @@ typedef struct pt_tuning {
     int32_t min_tris;        /* lanes with triangles pending that run a triangle step (0: per lane) */
     int32_t shade_variant;   /* surface shading stage: 0 unbounded registers, 1 at most 80, 2 at most 64 */
     float   frame_ms;        /* pt_autotune: device time of the tuned frame */
+    /* the first round of a frame (camera rays, coherent per warp, and the
+     * shadow rays of their hits) on its own: refill thresholds (0: as
+     * extend_refill / shadow_refill, else 1..32) and triangle-step quorums
+     * (-1: as min_tris, else 0..32) */
+    int32_t extend_refill_first;
+    int32_t min_tris_first;
+    int32_t shadow_refill_first;
+    int32_t shadow_min_tris_first;
 } pt_tuning;
 
 /* Autotuner: renders num_passes whole-frame passes (at least 2^23 paths:

@@ -24,14 +24,18 @@ def test_every_configuration_gives_the_same_image(ptlib, name):
         r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
         ref = None
         for variant, refill, min_tris in itertools.product(range(4), (1, 8, 32), (0, 8)):
+            # the first round on its own settings in half of the cases
+            first = dict(extend_refill_first=33 - refill, min_tris_first=4, shadow_refill_first=refill,
+                         shadow_min_tris_first=0) if variant % 2 else dict(
+                extend_refill_first=0, min_tris_first=-1, shadow_refill_first=0, shadow_min_tris_first=-1)
             r.set_tuning(extend_variant=variant, shadow_variant=3 - variant, extend_refill=refill,
-                         shadow_refill=refill, min_tris=min_tris, shade_variant=variant % 3)
+                         shadow_refill=refill, min_tris=min_tris, shade_variant=variant % 3, **first)
             r.clear()
             r.render_passes(0, 3)
             a = r.accum()
             if ref is None:
                 ref = a
-            assert np.array_equal(a, ref), (variant, refill, min_tris)
+            assert np.array_equal(a, ref), (variant, refill, min_tris, first)
 
 
 def test_autotune_keeps_the_accumulation(ptlib):
@@ -52,3 +56,7 @@ def test_autotune_keeps_the_accumulation(ptlib):
         assert np.array_equal(r.accum(), before)
         with pytest.raises(capi.PTError):
             r.set_tuning(extend_variant=7)
+        with pytest.raises(capi.PTError):
+            r.set_tuning(extend_refill_first=33)
+        with pytest.raises(capi.PTError):
+            r.set_tuning(min_tris_first=-2)
