@@ -1559,7 +1559,7 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
         // the shadow rays of their hits): refill threshold and quorum
         if (postpone) {
             const int rf[] = {20, 24, 28, 32};
-            const int mf[] = {2, 4, 6};
+            const int mf[] = {1, 2, 3, 4, 6};
             float be1 = 1e30f, bs1 = 1e30f;
             int re1 = 0, me1 = -1, rs1 = 0, ms1 = -1;
             for (int r : rf) {
@@ -1579,6 +1579,33 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
             if ((rc = measure(t, ms))) break;
             if (be1 < ms[STAGE_EXTEND]) { best.extend_refill_first = re1; best.min_tris_first = me1; }
             if (bs1 < ms[STAGE_SHADOW]) { best.shadow_refill_first = rs1; best.min_tris_shadow_first = ms1; }
+            // 6. the other rounds' refill thresholds and quorum again, now
+            // that they no longer set the first round's
+            const int refills[] = {8, 12, 16, 20, 24, 28};
+            float be2 = 1e30f, bs2 = 1e30f;
+            int re2 = best.extend_refill, rs2 = best.shadow_refill;
+            for (int r : refills) {
+                WavefrontTuning u = best;
+                u.extend_refill = u.shadow_refill = r;
+                if ((rc = measure(u, ms))) break;
+                if (ms[STAGE_EXTEND] < be2) { be2 = ms[STAGE_EXTEND]; re2 = r; }
+                if (ms[STAGE_SHADOW] < bs2) { bs2 = ms[STAGE_SHADOW]; rs2 = r; }
+            }
+            if (rc) break;
+            best.extend_refill = re2;
+            best.shadow_refill = rs2;
+            const int mins[] = {0, 4, 6, 8, 12};
+            float bt = 1e30f;
+            int mt = best.min_tris;
+            for (int m : mins) {
+                WavefrontTuning u = best;
+                u.min_tris = m;
+                if ((rc = measure(u, ms))) break;
+                const float tot = ms[STAGE_EXTEND] + ms[STAGE_SHADOW];
+                if (tot < bt) { bt = tot; mt = m; }
+            }
+            if (rc) break;
+            best.min_tris = mt;
         }
         if ((rc = measure(best, ms))) break;
     } while (false);

@@ -398,8 +398,9 @@ typedef struct pt_tuning {
  * untouched, with candidate configurations,
  * timing each stage with CUDA events, and keeps the fastest for this scene
  * and frame size.  Coordinate descent: kernel variants (extend and shadow
- * separately), refill thresholds (separately), min_tris, then the shading
- * stage's register budget. */
+ * separately), refill thresholds (separately), min_tris, the shading
+ * stage's register budget, then the first round's refill thresholds and
+ * quorums, and with those fixed the other rounds' again. */
 int pt_autotune(pt_context* ctx, int32_t num_passes, pt_tuning* result);
 int pt_get_tuning(pt_context* ctx, pt_tuning* tuning);
 int pt_set_tuning(pt_context* ctx, const pt_tuning* tuning);
