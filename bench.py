@@ -145,16 +145,17 @@ class ClockSampler:
 
 
 # DRAM bytes per closest-hit query of wf_extend on the icosphere workload:
-# dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch
-# (bounce 0 of a 1-spp frame, 2,073,600 camera rays) / its rays.  Traffic
-# grows with the rays of a launch: path-state reads and writes, BVH misses
-# in L2.
-EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 75.0}
+# dram__bytes_read.sum + dram__bytes_write.sum of all nine wf_extend launches
+# of one ncu-captured 1-spp frame (the autotuned launch configuration) / the
+# frame's 3.42 M closest-hit queries.  Traffic grows with the rays of a
+# launch: path-state reads and writes, BVH misses in L2.
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 88.2}
 # Warp-level instructions executed per closest-hit query by wf_extend on the
-# same ncu capture (smsp__inst_executed.sum of the launch / its rays): the
+# same capture (smsp__inst_executed.sum of the nine launches / the frame's
+# queries; camera rays take 190, the first bounce's rays 320): the
 # numerator of the instruction-issue roofline (4 warp instructions per cycle
 # per SM).
-EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 211.4}
+EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 239.6}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
