@@ -635,6 +635,7 @@ struct pt_batch {
     std::vector<pt_context*> jobs;
     std::vector<int> tlas_root, light_base;
     std::vector<BatchJob> entry;  // direct BLAS entry per job (direct, entry_inst, entry_mat)
+    std::vector<uint32_t> job_scene_flags;  // F_MEDIUM / F_ALPHA_TEST of each job's scene as copied
     uint32_t flags = 0;
     DevBuf<WideNode> nodes;
     DevBuf<WideTri> tris;
@@ -703,22 +704,22 @@ extern "C" {
 int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
     if (!jobs || n <= 0 || !out) return set_err(PT_ERR_INVALID_ARG, "invalid batch");
     *out = nullptr;
-    // each job keeps its own render options, environment map and texture
-    // maps; media and alpha-tested materials need the transmittance and
-    // inline any-hit stages, which batches do not run
-    const uint32_t unsupported = F_MEDIUM | F_ALPHA_TEST;
+    // each job keeps its own render options, environment map, texture maps,
+    // media and alpha-tested materials; a medium with volume MIS needs the
+    // transmittance stages, which batches do not run
     uint32_t flags = 0;
     for (int j = 0; j < n; ++j) {
         pt_context* c = jobs[j];
         if (!c) return set_err(PT_ERR_INVALID_ARG, "NULL job");
         if (c->device != jobs[0]->device) return set_err(PT_ERR_INVALID_ARG, "batch jobs must share a device");
         const uint32_t f = option_flags(c);
-        if (f & unsupported)
-            return set_err(PT_ERR_UNSUPPORTED, "batches take surface scenes (no media, no alpha-tested materials)");
+        if ((f & F_MEDIUM) && (f & F_VOL_MIS))
+            return set_err(PT_ERR_UNSUPPORTED, "batches take no medium with volume MIS");
         flags |= f;
     }
     pt_batch* b = new pt_batch;
     b->jobs.assign(jobs, jobs + n);
+    for (int j = 0; j < n; ++j) b->job_scene_flags.push_back(jobs[j]->scene_flags & (F_MEDIUM | F_ALPHA_TEST));
     b->device = jobs[0]->device;
     b->flags = flags;  // the union: which kernel forms the batch needs
     int rc = PT_OK;
@@ -819,6 +820,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     std::vector<BatchJob> base(n);
     std::vector<int> remaining(n);
     uint32_t flags = 0;  // union of the jobs' flags
+    bool inline_shadows = false;
     std::vector<long> job_paths(n);
     long total = 0, max_npix = 0;
     for (int j = 0; j < n; ++j) {
@@ -853,10 +855,14 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         J.accum = c->accum.p;
         J.npix = J.width * J.height;
         J.id = j;
-        // the job's options now; the scene flags of its copy in the batch
-        // (pt_batch_create took no media and no alpha-tested materials)
-        J.flags = option_flags(c) & ~(uint32_t)(F_MEDIUM | F_ALPHA_TEST);
+        // the job's options now, with the scene flags of its copy in the
+        // batch (those of pt_batch_create)
+        J.flags = (option_flags(c) & ~(uint32_t)(F_MEDIUM | F_ALPHA_TEST)) | (b->job_scene_flags[j]);
+        if ((J.flags & F_MEDIUM) && (J.flags & F_VOL_MIS))
+            return set_err(PT_ERR_UNSUPPORTED, "pt_batch_render: a medium with volume MIS");
         flags |= J.flags;
+        // AnyHit of an alpha-tested scene without media draws random numbers
+        if ((J.flags & F_ALPHA_TEST) && !(J.flags & F_MEDIUM)) inline_shadows = true;
         J.mollify_amt = o.roughness_mollification_amt;
         for (int k = 0; k < 3; ++k) J.uniform_light[k] = o.uniform_light_col[k];
         J.env = c->env.p;
@@ -961,7 +967,8 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         const cudaError_t ce =
-            launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches);
+            launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches,
+                         inline_shadows);
         const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
         if (ce != cudaSuccess || ee != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -989,7 +996,8 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         CK(cudaEventRecord(b->ev1, b->stream));
     } else {
         CK(cudaEventRecord(b->ev0, b->stream));
-        CK(launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches));
+        CK(launch_batch(p, chunks.data(), (int)chunks.size(), b->wf, t, b->stream, b->done.p + n, &launches,
+                        inline_shadows));
         CK(cudaEventRecord(b->ev1, b->stream));
     }
     std::vector<unsigned long long> done(n + 1);

@@ -655,7 +655,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
                 V3 envCol = EvalEnvMap(P, ps.r, envPdf);
                 float misWeight = 1.0f;
                 if (ps.depth > 0) misWeight = PowerHeuristic(ps.scatterPdf, envPdf);
-                if (MEDIUM == 1 && !ps.surfaceScatter) misWeight = 1.0f;
+                if (MEDIUM == 1 && (F & F_MEDIUM) && !ps.surfaceScatter) misWeight = 1.0f;
                 if (misWeight > 0.0f) ps.radiance = ps.radiance + misWeight * envCol * ps.throughput * P.env_intensity;
             }
         }
@@ -677,7 +677,7 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
     if ((F & F_LIGHTS) && hr.isEmitter) {
         float misWeight = 1.0f;
         if (ps.depth > 0) misWeight = PowerHeuristic(ps.scatterPdf, hr.lightPdf);
-        if (MEDIUM == 1 && !ps.surfaceScatter) misWeight = 1.0f;
+        if (MEDIUM == 1 && (F & F_MEDIUM) && !ps.surfaceScatter) misWeight = 1.0f;
         hook.emitter(ps, misWeight, hr);
         ps.radiance = ps.radiance + misWeight * hr.lightEmission * ps.throughput;
         return false;
@@ -685,7 +685,9 @@ __device__ __forceinline__ bool ShadeStep(const Params& P, PathState& ps, const 
     if (ps.depth == P.max_depth) return false;
     bool mediumSampled = false;
     V3 scatterL = v3(0.0f);
-    if (MEDIUM) {
+    // MEDIUM: the scene may have media (OPT_MEDIUM); a batch's job without
+    // any (F_MEDIUM clear) takes the MEDIUM == 0 path at run time
+    if (MEDIUM && (F & F_MEDIUM)) {
         ps.surfaceScatter = false;
         if (ps.inMedium) {
             if (ps.medium.type == MEDIUM_ABSORB) {

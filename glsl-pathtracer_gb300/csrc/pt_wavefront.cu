@@ -986,6 +986,20 @@ __global__ void __launch_bounds__(128, MINB) wf_transmit(Params P, WfView B, int
 // megakernel's loop at PT_MAX_PATH_ITERATIONS per path in all (`rounds`
 // done in the wavefront rounds).
 template <int MEDIUM, bool ENV>
+__device__ __forceinline__ void tail_path(const Params& P, PathState& ps, int rounds, uint2* stack, Counters& cnt) {
+    for (int guard = rounds;;) {
+        if (++guard > PT_MAX_PATH_ITERATIONS) {
+            count_truncated(P);
+            break;
+        }
+        HitRecord hr;
+        TraceClosest(P, ps.r, ps.depth, hr, stack, cnt, false);
+        ShadowReq sr;
+        NoHook nh;
+        if (!ShadeStep<MEDIUM, ENV, true>(P, ps, hr, sr, stack, cnt, nh)) break;
+    }
+}
+template <int MEDIUM, bool ENV, bool BATCH = false>
 __global__ void __launch_bounds__(128) wf_tail(Params P, WfView B, int in, int rounds) {
     uint2 stack[kStackSize];
     const int n = B.counts[in];
@@ -994,18 +1008,15 @@ __global__ void __launch_bounds__(128) wf_tail(Params P, WfView B, int in, int r
         const int i = B.q[in][j];
         PathState ps;
         load_path(B, i, ps);
-        for (int guard = rounds;;) {
-            if (++guard > PT_MAX_PATH_ITERATIONS) {
-                count_truncated(P);
-                break;
-            }
-            HitRecord hr;
-            TraceClosest(P, ps.r, ps.depth, hr, stack, cnt, false);
-            ShadowReq sr;
-            NoHook nh;
-            if (!ShadeStep<MEDIUM, ENV, true>(P, ps, hr, sr, stack, cnt, nh)) break;
+        if constexpr (BATCH) {
+            Params Pj = P;
+            job_params(Pj, P.jobs[ps.job]);
+            tail_path<MEDIUM, ENV>(Pj, ps, rounds, stack, cnt);
+        } else {
+            tail_path<MEDIUM, ENV>(P, ps, rounds, stack, cnt);
         }
         B.rad[i] = make_float4(ps.radiance.x, ps.radiance.y, ps.radiance.z, ps.alpha);
+        if (BATCH) job_path_done(P, ps.job);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
 }
@@ -1654,8 +1665,51 @@ cudaError_t launch_adjoint(const Params& p, const RenderWork& W, WavefrontBuffer
     return cudaSuccess;
 }
 
+// The shade form of a batch: media without volume MIS (MEDIUM 1) when a job
+// has a medium, the environment-map code when a job has a map, shadow rays
+// traced inline when a job has alpha-tested materials and no medium (its
+// AnyHit draws random numbers); each path takes its job's own flags at run
+// time within that form.
+template <int MEDIUM, bool ENV, bool INLINE>
+static cudaError_t batch_shade(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
+    if (MEDIUM == 0 && !INLINE) {
+        const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
+        return launch_shade_plain<true, ENV>(p, v, in, t.shade_variant, g3, t.shade_block, s);
+    }
+    wf_shade<MEDIUM, ENV, INLINE, false, 1, false, true><<<t.shade_grid, t.shade_block, 0, s>>>(p, v, in, RenderWork{},
+                                                                                             AdjView{});
+    return cudaGetLastError();
+}
+static cudaError_t batch_shade_dispatch(const Params& p, const WfView& v, int in, const WavefrontTuning& t,
+                                        bool inline_shadows, cudaStream_t s) {
+    const int medium = (p.flags & F_MEDIUM) ? 1 : 0;
+    const bool env = (p.flags & F_ENVMAP) != 0;
+    switch (medium * 4 + (env ? 2 : 0) + (inline_shadows ? 1 : 0)) {
+        case 0: return batch_shade<0, false, false>(p, v, in, t, s);
+        case 1: return batch_shade<0, false, true>(p, v, in, t, s);
+        case 2: return batch_shade<0, true, false>(p, v, in, t, s);
+        case 3: return batch_shade<0, true, true>(p, v, in, t, s);
+        case 4: return batch_shade<1, false, false>(p, v, in, t, s);
+        case 5: return batch_shade<1, false, true>(p, v, in, t, s);
+        case 6: return batch_shade<1, true, false>(p, v, in, t, s);
+        default: return batch_shade<1, true, true>(p, v, in, t, s);
+    }
+}
+static cudaError_t batch_tail(const Params& p, const WfView& v, int in, int rounds, int grid, cudaStream_t s) {
+    const int medium = (p.flags & F_MEDIUM) ? 1 : 0;
+    const bool env = (p.flags & F_ENVMAP) != 0;
+    switch (medium * 2 + (env ? 1 : 0)) {
+        case 0: wf_tail<0, false, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 1: wf_tail<0, true, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        case 2: wf_tail<1, false, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+        default: wf_tail<1, true, true><<<grid, 128, 0, s>>>(p, v, in, rounds); break;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chunks, WavefrontBuffers& wb,
-                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp, int* launches) {
+                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp, int* launches,
+                         bool inline_shadows) {
     int dummy = 0;
     int& nl = launches ? *launches : dummy;
     nl = 0;
@@ -1674,23 +1728,25 @@ cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chun
         const int gen_grid = std::min((ch.paths + 255) / 256, t.resident_blocks_256);
         wf_generate<true><<<gen_grid, 256, 0, s>>>(pc, RenderWork{}, v, 0, 0, ch.paths);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        // batches take surface scenes (no media, no alpha test): the plain
-        // shade, with the environment-map code when a job has a map
-        const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
-        const bool env = (p.flags & F_ENVMAP) != 0;
-        for (int it = 0; it <= ch.max_depth; ++it) {
+        // alpha pass-through keeps a path at the same depth: as for a single
+        // scene (enqueue_batch), more rounds and then the tail kernel
+        const bool linger = (p.flags & F_ALPHA_TEST) != 0;
+        const int rounds = ch.max_depth + 1 + (linger ? kExtraRounds : 0);
+        for (int it = 0; it < rounds; ++it) {
             const int in = it & 1;
-            if ((e = launch_extend<true>(pc, v, with_first_round(in, it == 0), t, s)) != cudaSuccess) return e;
             const int sin = with_first_round(in, it == 0);
-            if ((e = env ? launch_shade_plain<true, true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)
-                         : launch_shade_plain<true>(pc, v, sin, t.shade_variant, g3, t.shade_block, s)) != cudaSuccess)
-                return e;
+            if ((e = launch_extend<true>(pc, v, sin, t, s)) != cudaSuccess) return e;
+            if ((e = batch_shade_dispatch(pc, v, sin, t, inline_shadows, s)) != cudaSuccess) return e;
             if ((e = launch_shadow<false, true>(pc, v, t, AdjView{}, 0, s, it == 0)) != cudaSuccess) return e;
+        }
+        if (linger) {
+            if ((e = batch_tail(pc, v, rounds & 1, rounds, t.shade_grid, s)) != cudaSuccess) return e;
+            ++nl;
         }
         const int res_grid = std::min((ch.pixels + 255) / 256, t.resident_blocks_256);
         wf_resolve_batch<<<res_grid, 256, 0, s>>>(pc, v, ch.pixels);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        nl += 2 + 3 * (ch.max_depth + 1);
+        nl += 2 + 3 * rounds;
     }
     return cudaSuccess;
 }

@@ -130,8 +130,8 @@ struct BatchChunk {
 // p.jobs: the whole entry table; p.job_remaining / p.job_done: indexed by
 // BatchJob::id.  start_stamp receives the global timer at the start.
 cudaError_t launch_batch(const Params& p, const BatchChunk* chunks, int num_chunks, WavefrontBuffers& wb,
-                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp,
-                         int* launches = nullptr);
+                         const WavefrontTuning& t, cudaStream_t s, unsigned long long* start_stamp, int* launches,
+                         bool inline_shadows);
 
 // *launches (if given) receives the number of kernels launched; with a
 // timer, every launch is timed (and no graph is used).

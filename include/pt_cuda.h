@@ -206,9 +206,9 @@ int pt_gpu_build_ms(pt_context* ctx, float* ms);
  * batch kernels' separately compiled arithmetic.
  * Jobs share one device.  Each keeps its own render options (Russian
  * roulette, hidden emitters, background, uniform light, roughness
- * mollification, normal-map convention ...), environment map and texture
- * maps; scenes with a medium or alpha-tested materials are refused
- * (PT_ERR_UNSUPPORTED).  The batch launches with the tuning (pt_autotune /
+ * mollification, normal-map convention ...), environment map, texture maps,
+ * alpha-tested materials and media; a medium with volume MIS
+ * (enable_volume_mis) is refused (PT_ERR_UNSUPPORTED).  The batch launches with the tuning (pt_autotune /
  * pt_set_tuning) of the first job that has one, else the default.  The
  * contexts must outlive the batch: environment and texture maps are read
  * from them in place.  Scene, material and light updates made to a context

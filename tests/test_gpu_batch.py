@@ -197,13 +197,50 @@ def test_batch_jobs_with_own_options_and_maps(ptlib):
             r.close()
 
 
+def test_batch_jobs_with_alpha_and_media(ptlib):
+    """Alpha-tested materials (blend and mask, shadow rays traced inline
+    since their AnyHit draws random numbers, pass-through paths finished by
+    the tail kernel), absorbing and emissive media without volume MIS, an
+    environment map and a plain scene in one batch; each equals its own
+    render."""
+    from pathtracer import capi, scenes
+    from pathtracer.renderer import GpuBatch, GpuRenderer
+    jobs = [(golden_scene("ref_scene_textured.npz"), 0, 3),
+            (golden_scene("feature_scene_absorb.npz"), 1, 2),
+            (golden_scene("feature_scene_emissive.npz"), 0, 2),
+            (golden_scene("feature_scene_env_only.npz"), 2, 2),
+            (scenes.cornell(40, 24, max_depth=4), 0, 2)]
+    rs = [GpuRenderer(sd) for sd, _, _ in jobs]
+    try:
+        ref = []
+        for r, (sd, fp, n) in zip(rs, jobs):
+            r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+            r.clear()
+            r.render_passes(fp, n)
+            ref.append(r.accum())
+            r.clear()
+        with GpuBatch(rs) as b:
+            b.render([fp for _, fp, _ in jobs], [n for _, _, n in jobs])
+            st = b.stats()
+        assert st["status"] == 0
+        assert st["paths"] == sum(r.width * r.height * n for r, (_, _, n) in zip(rs, jobs))
+        for k, (r, a) in enumerate(zip(rs, ref)):
+            got = r.accum()
+            frac, mean_rel = image_agreement(got, a)
+            assert frac >= 0.999 and mean_rel < 1e-4, (k, frac, mean_rel)
+            assert np.array_equal(got[..., 3], a[..., 3])
+    finally:
+        for r in rs:
+            r.close()
+
+
 def test_batch_rejects_unsupported_jobs(ptlib):
     from pathtracer import capi, scenes
     from pathtracer.renderer import GpuBatch, GpuRenderer
     a = GpuRenderer(scenes.cornell(16, 16), **COMMON)
     env = scenes.instanced_scene(num_instances=20, tris_per_blas=500, width=16, height=16, env_size=(32, 16))
-    b = GpuRenderer(env)  # a medium
-    c = GpuRenderer(golden_scene("ref_scene_textured.npz"))  # alpha-tested materials
+    b = GpuRenderer(env)  # a medium with volume MIS
+    c = GpuRenderer(golden_scene("feature_scene_absorb_volmis.npz"))  # the same
     try:
         for pair in ([a, b], [a, c]):
             with pytest.raises(capi.PTError) as e:
