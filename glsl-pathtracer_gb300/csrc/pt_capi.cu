@@ -1459,6 +1459,8 @@ void tuning_out(const WavefrontTuning& t, float ms, pt_tuning* out) {
     out->min_tris_first = t.min_tris_first;
     out->shadow_refill_first = t.shadow_refill_first;
     out->shadow_min_tris_first = t.min_tris_shadow_first;
+    out->extend_variant_first = t.extend_variant_first;
+    out->shade_variant_first = t.shade_variant_first;
 }
 }  // namespace
 
@@ -1615,6 +1617,31 @@ int pt_autotune(pt_context* c, int32_t num_passes, pt_tuning* out) {
             if (rc) break;
             best.min_tris = mt;
         }
+        // 7. the first round's extend kernel variant and shading budget
+        {
+            WavefrontTuning t = best;
+            if ((rc = measure(t, ms))) break;
+            float be3 = ms[STAGE_EXTEND], bsh3 = ms[STAGE_SHADE];
+            int ve3 = -1, vs3 = -1;
+            for (int v = 0; v < 4; ++v) {
+                if (v == best.extend_variant) continue;
+                WavefrontTuning u = best;
+                u.extend_variant_first = v;
+                if ((rc = measure(u, ms))) break;
+                if (ms[STAGE_EXTEND] < be3) { be3 = ms[STAGE_EXTEND]; ve3 = v; }
+            }
+            if (rc) break;
+            for (int v = 0; v < 3; ++v) {
+                if (v == best.shade_variant) continue;
+                WavefrontTuning u = best;
+                u.shade_variant_first = v;
+                if ((rc = measure(u, ms))) break;
+                if (ms[STAGE_SHADE] < bsh3) { bsh3 = ms[STAGE_SHADE]; vs3 = v; }
+            }
+            if (rc) break;
+            best.extend_variant_first = ve3;
+            best.shade_variant_first = vs3;
+        }
         if ((rc = measure(best, ms))) break;
     } while (false);
     timer.release();
@@ -1646,7 +1673,8 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
         in->min_tris < 0 || in->min_tris > 32 || in->shade_variant < 0 || in->shade_variant > 2 ||
         in->extend_refill_first < 0 || in->extend_refill_first > 32 || in->shadow_refill_first < 0 ||
         in->shadow_refill_first > 32 || in->min_tris_first < -1 || in->min_tris_first > 32 ||
-        in->shadow_min_tris_first < -1 || in->shadow_min_tris_first > 32)
+        in->shadow_min_tris_first < -1 || in->shadow_min_tris_first > 32 || in->extend_variant_first < -1 ||
+        in->extend_variant_first > 3 || in->shade_variant_first < -1 || in->shade_variant_first > 2)
         return set_err(PT_ERR_INVALID_ARG, "tuning value out of range");
     if (!c->wf_tuned) {
         CK(wavefront_default_tuning(c->wf_tuning, 128));
@@ -1662,6 +1690,8 @@ int pt_set_tuning(pt_context* c, const pt_tuning* in) {
     c->wf_tuning.min_tris_first = in->min_tris_first;
     c->wf_tuning.shadow_refill_first = in->shadow_refill_first;
     c->wf_tuning.min_tris_shadow_first = in->shadow_min_tris_first;
+    c->wf_tuning.extend_variant_first = in->extend_variant_first;
+    c->wf_tuning.shade_variant_first = in->shade_variant_first;
     return PT_OK;
 }
 

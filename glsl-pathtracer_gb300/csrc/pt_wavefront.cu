@@ -1388,16 +1388,17 @@ static cudaError_t launch_transmit_replay(const Params& p, const WfView& v, cons
 
 template <bool BATCH = false>
 static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
-    const int g = t.extend_grid_v[t.extend_variant];
     // the first round's camera rays (coherent 8 x 4 blocks) may take their own
-    // refill threshold and triangle-step quorum
+    // kernel variant, refill threshold and triangle-step quorum
     const bool first = (in & kFirstRound) != 0;
+    const int var = first && t.extend_variant_first >= 0 ? t.extend_variant_first : t.extend_variant;
+    const int g = t.extend_grid_v[var];
     const int b = t.extend_block;
     const int r = first && t.extend_refill_first > 0 ? t.extend_refill_first : t.extend_refill;
     const int m = first && t.min_tris_first >= 0 ? t.min_tris_first : t.min_tris;
     // a batch takes the direct form when every job enters directly (p.direct)
     if (p.direct) {
-        switch (t.extend_variant) {
+        switch (var) {
             case 1: wf_extend<8, true, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
             case 2: wf_extend<6, false, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
             case 3: wf_extend<6, true, BATCH, true><<<g, b, 0, s>>>(p, v, in, r, m); break;
@@ -1405,7 +1406,7 @@ static cudaError_t launch_extend(const Params& p, const WfView& v, int in, const
         }
         return cudaGetLastError();
     }
-    switch (t.extend_variant) {
+    switch (var) {
         case 1: wf_extend<8, true, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
         case 2: wf_extend<6, false, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
         case 3: wf_extend<6, true, BATCH><<<g, b, 0, s>>>(p, v, in, r, m); break;
@@ -1531,7 +1532,9 @@ static cudaError_t enqueue_bounce(const Params& p, const WfView& v, int in, cons
     }
     if ((e = timed(timer, STAGE_SHADE, s,
                    [&] {
-                       return shade_dispatch(p, v, sin, t.shade_grid, t.shade_block, s, t.shade_variant,
+                       return shade_dispatch(p, v, sin, t.shade_grid, t.shade_block, s,
+                                             first && t.shade_variant_first >= 0 ? t.shade_variant_first
+                                                                                 : t.shade_variant,
                                              t.shade_grid_v);
                    })) != cudaSuccess)
         return e;
@@ -1674,7 +1677,8 @@ template <int MEDIUM, bool ENV, bool INLINE>
 static cudaError_t batch_shade(const Params& p, const WfView& v, int in, const WavefrontTuning& t, cudaStream_t s) {
     if (MEDIUM == 0 && !INLINE) {
         const int g3[3] = {t.shade_grid, t.shade_grid_v[1], t.shade_grid_v[2]};
-        return launch_shade_plain<true, ENV>(p, v, in, t.shade_variant, g3, t.shade_block, s);
+        const int var = (in & kFirstRound) && t.shade_variant_first >= 0 ? t.shade_variant_first : t.shade_variant;
+        return launch_shade_plain<true, ENV>(p, v, in, var, g3, t.shade_block, s);
     }
     wf_shade<MEDIUM, ENV, INLINE, false, 1, false, true><<<t.shade_grid, t.shade_block, 0, s>>>(p, v, in, RenderWork{},
                                                                                              AdjView{});
@@ -1806,6 +1810,14 @@ cudaError_t wavefront_default_tuning(WavefrontTuning& t, int block) {
     if (const char* r = std::getenv("PT_WAVEFRONT_VARIANT")) {
         const int v = std::atoi(r);
         if (v >= 0 && v < 4) t.extend_variant = t.shadow_variant = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_VARIANT_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v < 4) t.extend_variant_first = v;
+    }
+    if (const char* r = std::getenv("PT_WAVEFRONT_SHADE_VARIANT_FIRST")) {
+        const int v = std::atoi(r);
+        if (v >= 0 && v < 3) t.shade_variant_first = v;
     }
     if (const char* r = std::getenv("PT_WAVEFRONT_REFILL_FIRST")) {
         const int v = std::atoi(r);

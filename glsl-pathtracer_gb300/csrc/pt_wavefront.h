@@ -48,6 +48,10 @@ struct WavefrontTuning {
     // PT_WAVEFRONT_SHADOW_REFILL_FIRST, PT_WAVEFRONT_SHADOW_MIN_TRIS_FIRST)
     int extend_refill_first = 0, min_tris_first = -1;
     int shadow_refill_first = 0, min_tris_shadow_first = -1;
+    // and the first round's extend kernel variant and shading register
+    // budget (-1: as the other rounds; PT_WAVEFRONT_VARIANT_FIRST,
+    // PT_WAVEFRONT_SHADE_VARIANT_FIRST)
+    int extend_variant_first = -1, shade_variant_first = -1;
     int extend_grid = 0, shade_grid = 0, shadow_grid = 0;
     // kernel variants of the traversal stages: 0 = 8 blocks (64 registers),
     // scalar node test; 1 = 8 blocks, packed; 2 = 6 blocks (80 registers),

@@ -87,7 +87,8 @@ class pt_tuning(C.Structure):
     _fields_ = [("extend_variant", C.c_int32), ("shadow_variant", C.c_int32), ("extend_refill", C.c_int32),
                 ("shadow_refill", C.c_int32), ("min_tris", C.c_int32), ("shade_variant", C.c_int32),
                 ("frame_ms", C.c_float), ("extend_refill_first", C.c_int32), ("min_tris_first", C.c_int32),
-                ("shadow_refill_first", C.c_int32), ("shadow_min_tris_first", C.c_int32)]
+                ("shadow_refill_first", C.c_int32), ("shadow_min_tris_first", C.c_int32),
+                ("extend_variant_first", C.c_int32), ("shade_variant_first", C.c_int32)]
 
 
 class pt_stage_stats(C.Structure):

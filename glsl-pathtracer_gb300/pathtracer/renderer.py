@@ -146,7 +146,7 @@ class GpuRenderer:
 
     TUNING_FIELDS = ("extend_variant", "shadow_variant", "extend_refill", "shadow_refill", "min_tris",
                      "shade_variant", "extend_refill_first", "min_tris_first", "shadow_refill_first",
-                     "shadow_min_tris_first")
+                     "shadow_min_tris_first", "extend_variant_first", "shade_variant_first")
 
     def autotune(self, num_passes: int = 2) -> dict:
         t = capi.pt_tuning()

@@ -391,6 +391,8 @@ typedef struct pt_tuning {
     int32_t min_tris_first;
     int32_t shadow_refill_first;
     int32_t shadow_min_tris_first;
+    int32_t extend_variant_first;  /* -1: as extend_variant, else 0..3 */
+    int32_t shade_variant_first;   /* -1: as shade_variant, else 0..2 */
 } pt_tuning;
 
 /* Autotuner: renders num_passes whole-frame passes (at least 2^23 paths:
@@ -400,7 +402,8 @@ typedef struct pt_tuning {
  * and frame size.  Coordinate descent: kernel variants (extend and shadow
  * separately), refill thresholds (separately), min_tris, the shading
  * stage's register budget, then the first round's refill thresholds and
- * quorums, and with those fixed the other rounds' again. */
+ * quorums, and with those fixed the other rounds' again, then the first
+ * round's extend variant and shading budget. */
 int pt_autotune(pt_context* ctx, int32_t num_passes, pt_tuning* result);
 int pt_get_tuning(pt_context* ctx, pt_tuning* tuning);
 int pt_set_tuning(pt_context* ctx, const pt_tuning* tuning);

@@ -26,8 +26,10 @@ def test_every_configuration_gives_the_same_image(ptlib, name):
         for variant, refill, min_tris in itertools.product(range(4), (1, 8, 32), (0, 8)):
             # the first round on its own settings in half of the cases
             first = dict(extend_refill_first=33 - refill, min_tris_first=4, shadow_refill_first=refill,
-                         shadow_min_tris_first=0) if variant % 2 else dict(
-                extend_refill_first=0, min_tris_first=-1, shadow_refill_first=0, shadow_min_tris_first=-1)
+                         shadow_min_tris_first=0, extend_variant_first=(variant + 1) % 4,
+                         shade_variant_first=(variant + 2) % 3) if variant % 2 else dict(
+                extend_refill_first=0, min_tris_first=-1, shadow_refill_first=0, shadow_min_tris_first=-1,
+                extend_variant_first=-1, shade_variant_first=-1)
             r.set_tuning(extend_variant=variant, shadow_variant=3 - variant, extend_refill=refill,
                          shadow_refill=refill, min_tris=min_tris, shade_variant=variant % 3, **first)
             r.clear()
@@ -60,3 +62,5 @@ def test_autotune_keeps_the_accumulation(ptlib):
             r.set_tuning(extend_refill_first=33)
         with pytest.raises(capi.PTError):
             r.set_tuning(min_tris_first=-2)
+        with pytest.raises(capi.PTError):
+            r.set_tuning(extend_variant_first=4)
