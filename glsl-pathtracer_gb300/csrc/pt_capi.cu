@@ -90,6 +90,7 @@ struct pt_context {
     DevBuf<InstRef> insts;
     DevBuf<InstXf> xf;
     DevBuf<uint4> inst_bounds;  // root_may_hit's bounds per InstRef (empty: no culling)
+    DevBuf<uint4> node_words;   // each wide node's per-slot hit-mask words
     DevBuf<int32_t> vidx;
     DevBuf<float4> verts, norms, mats, lights, env;
     DevBuf<float> cdf;
@@ -154,6 +155,35 @@ __global__ void k_inst_bounds(const WideNode* __restrict__ nodes, const InstRef*
     out[2 * i + 1] = make_uint4(lo[0] | lo[1] << 8 | lo[2] << 16, hi[0] | hi[1] << 8 | hi[2] << 16, 0u, 0u);
 }
 
+// Per wide node, the word each slot adds to the node test's hit mask
+// (intersect_node): a leaf child's triangle (or instance) bits at its
+// offset, an internal child's bit 24 + slot, 0 for an empty slot.
+__global__ void k_node_words(const WideNode* __restrict__ nodes, int count, uint4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint32_t w[8];
+    for (int slot = 0; slot < 8; ++slot) {
+        const uint32_t m = (nodes[i].w[6 + (slot >> 2)] >> (8 * (slot & 3))) & 0xffu;
+        const bool inner = ((m & (m << 1)) & 0x10u) != 0;
+        w[slot] = m == 0 ? 0u : inner ? 1u << (24 + slot) : (m >> 5) << (m & 0x1fu);
+    }
+    out[2 * i] = make_uint4(w[0], w[1], w[2], w[3]);
+    out[2 * i + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+cudaError_t make_node_words(DevBuf<uint4>& out, const WideNode* nodes, int count, cudaStream_t s) {
+    if (count <= 0) {
+        out.free();
+        return cudaSuccess;
+    }
+    if (out.n != 2 * (size_t)count) {
+        cudaError_t e = out.alloc(2 * (size_t)count);
+        if (e != cudaSuccess) return e;
+    }
+    k_node_words<<<(count + 255) / 256, 256, 0, s>>>(nodes, count, out.p);
+    return cudaGetLastError();
+}
+
 bool instance_culling_enabled() {
     const char* v = std::getenv("PT_INSTANCE_BOUNDS");
     return !(v && v[0] == '0');
@@ -197,6 +227,7 @@ Params make_params(const pt_context* c) {
     p.insts = reinterpret_cast<const int4*>(c->insts.p);
     p.xf = reinterpret_cast<const float4*>(c->xf.p);
     p.inst_bounds = c->inst_bounds.p;
+    p.node_words = c->node_words.p;
     p.tlas_root = c->bvh.tlas_root;
     if (c->direct) {
         p.tlas_root = c->entry.blas_root;
@@ -299,6 +330,7 @@ int upload_bvh(pt_context* c) {
     CK(c->tris.upload(c->bvh.tris, c->bvh.num_tris, c->stream));
     CK(c->insts.upload(c->bvh.insts, c->bvh.num_inst_refs, c->stream));
     CK(make_inst_bounds(c->inst_bounds, c->nodes.p, c->insts.p, c->bvh.num_inst_refs, c->stream));
+    CK(make_node_words(c->node_words, c->nodes.p, c->bvh.num_nodes, c->stream));
     c->direct = c->bvh.num_inst_refs == 1 && c->bvh.insts[0].identity;
     if (c->direct) c->entry = c->bvh.insts[0];
     const int need = trav_stack_need(c->bvh.tlas_depth, c->bvh.blas_depth, c->direct);
@@ -479,6 +511,7 @@ int gpu_rebuild(pt_context* c, const float* transforms) {
     c->bvh.num_tris = g.num_tris;
     c->bvh.num_inst_refs = g.num_insts;
     CK(make_inst_bounds(c->inst_bounds, c->nodes.p, c->insts.p, g.num_insts, c->stream));
+    CK(make_node_words(c->node_words, c->nodes.p, g.num_nodes, c->stream));
     c->direct = false;
     if (g.num_insts == 1) {
         InstRef r;
@@ -642,6 +675,7 @@ struct pt_batch {
     DevBuf<InstRef> insts;
     DevBuf<InstXf> xf;
     DevBuf<uint4> inst_bounds;
+    DevBuf<uint4> node_words;
     DevBuf<int32_t> vidx;
     DevBuf<float4> verts, norms, mats, lights;
     DevBuf<BatchJob> job_table;
@@ -792,6 +826,7 @@ int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
             light_off += (int)(c->lights.n / 4);  // a job without lights holds one padding record
         }
         if (e == cudaSuccess) e = make_inst_bounds(b->inst_bounds, b->nodes.p, b->insts.p, ref_off, b->stream);
+        if (e == cudaSuccess) e = make_node_words(b->node_words, b->nodes.p, node_off, b->stream);
         if (e != cudaSuccess) { rc = cuda_err(e, "batch index fix-up"); break; }
         if ((e = b->counters.alloc(4)) != cudaSuccess || (e = b->status.alloc(1)) != cudaSuccess ||
             (e = b->remaining.alloc(n)) != cudaSuccess || (e = b->done.alloc(n + 1)) != cudaSuccess) {
@@ -935,6 +970,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.insts = reinterpret_cast<const int4*>(b->insts.p);
     p.xf = reinterpret_cast<const float4*>(b->xf.p);
     p.inst_bounds = b->inst_bounds.p;
+    p.node_words = b->node_words.p;
     p.vidx = b->vidx.p;
     p.verts = b->verts.p;
     p.norms = b->norms.p;
@@ -1034,7 +1070,7 @@ int pt_batch_stats(pt_batch* b, pt_stats* s) {
 int pt_batch_destroy(pt_batch* b) {
     if (!b) return PT_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    b->nodes.free(); b->tris.free(); b->insts.free(); b->xf.free(); b->inst_bounds.free(); b->vidx.free(); b->verts.free();
+    b->nodes.free(); b->tris.free(); b->insts.free(); b->xf.free(); b->inst_bounds.free(); b->node_words.free(); b->vidx.free(); b->verts.free();
     b->norms.free(); b->mats.free(); b->lights.free(); b->job_table.free(); b->remaining.free(); b->done.free();
     b->counters.free(); b->status.free();
     wavefront_free(b->wf);
@@ -1055,7 +1091,7 @@ int pt_gpu_build_ms(pt_context* c, float* ms) {
 int pt_destroy(pt_context* c) {
     if (!c) return PT_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->inst_bounds.free(); c->vidx.free(); c->verts.free();
+    c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->inst_bounds.free(); c->node_words.free(); c->vidx.free(); c->verts.free();
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
     c->tex.free();
     c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();

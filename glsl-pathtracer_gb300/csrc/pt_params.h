@@ -61,6 +61,7 @@ struct Params {
     const int4* insts;      // InstRef
     const float4* xf;       // InstXf, 10 x float4 per instance
     const uint4* inst_bounds;  // 2 x uint4 per InstRef (root_may_hit); null: every instance is entered
+    const uint4* node_words;   // 2 x uint4 per wide node: each slot's hit-mask word (intersect_node)
     int tlas_root;
     // direct != 0: the scene is one untransformed instance, and traversal
     // starts in its BLAS (tlas_root is then the BLAS root) as instance

@@ -151,27 +151,23 @@ __device__ __forceinline__ NodeFrame node_frame(uint4 w0, const TRay& r) {
 // max / min (sm_100+).  PACKED computes the near and far planes of an axis
 // as one packed pair (the same values, fewer instructions, more registers).
 template <bool PACKED = false>
-__device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, int idx, const TRay& r,
-                                                   float tmax, uint32_t& child_base, uint32_t& prim_base,
-                                                   uint32_t& imask) {
+__device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nodes, const uint4* __restrict__ words,
+                                                   int idx, const TRay& r, float tmax, uint32_t& child_base,
+                                                   uint32_t& prim_base, uint32_t& imask) {
     const uint4* n = nodes + (size_t)idx * 5;
     const uint4 w0 = __ldg(n), w1 = __ldg(n + 1), w2 = __ldg(n + 2), w3 = __ldg(n + 3), w4 = __ldg(n + 4);
+    const uint4 hw0 = __ldg(words + 2 * (size_t)idx), hw1 = __ldg(words + 2 * (size_t)idx + 1);
     imask = w0.w >> 24;
     child_base = w1.x;
     prim_base = w1.y;
     const NodeFrame f = node_frame(w0, r);
     const float adjx = f.adjx, adjy = f.adjy, adjz = f.adjz;
     const float cnx = f.cnx, cfx = f.cfx, cny = f.cny, cfy = f.cfy, cnz = f.cnz, cfz = f.cfz;
-    const uint32_t oct_inv4 = r.oct_inv * 0x01010101u;
     const bool nx = !(r.oct_inv & 1u), ny = !(r.oct_inv & 2u), nz = !(r.oct_inv & 4u);
     uint32_t hits = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
-        const uint32_t meta4 = half ? w1.w : w1.z;
-        const uint32_t is_inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
-        const uint32_t inner_mask4 = (is_inner4 >> 4) * 0xffu;
-        const uint32_t bit_index4 = (meta4 ^ (oct_inv4 & inner_mask4)) & 0x1f1f1f1fu;
-        const uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
+        const uint4 hw = half ? hw1 : hw0;
         const uint32_t qlox = half ? w2.y : w2.x, qloy = half ? w2.w : w2.z, qloz = half ? w3.y : w3.x;
         const uint32_t qhix = half ? w3.w : w3.z, qhiy = half ? w4.y : w4.x, qhiz = half ? w4.w : w4.z;
         const uint32_t nxw = nx ? qhix : qlox, fxw = nx ? qlox : qhix;
@@ -197,14 +193,20 @@ __device__ __forceinline__ uint32_t intersect_node(const uint4* __restrict__ nod
             }
             const float t0 = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
             const float t1 = fmin3f(tfx, tfy, fminf(tfz, tmax));
-            if (t0 <= t1) {
-                const uint32_t cb = (child_bits4 >> (8 * j)) & 0xffu;
-                const uint32_t bi = (bit_index4 >> (8 * j)) & 0xffu;
-                hits |= cb << bi;
-            }
+            if (t0 <= t1) hits |= (j == 0 ? hw.x : j == 1 ? hw.y : j == 2 ? hw.z : hw.w);
         }
     }
-    return hits;
+    // internal children: from slot order to the ray's visiting order (bit
+    // 24 + (slot ^ oct_inv)), swapping bit pairs, bit quads and nibbles
+    uint32_t in8 = hits >> 24;
+    const uint32_t o = r.oct_inv;
+    uint32_t t = ((in8 & 0x55u) << 1) | ((in8 >> 1) & 0x55u);
+    in8 = (o & 1u) ? t : in8;
+    t = ((in8 & 0x33u) << 2) | ((in8 >> 2) & 0x33u);
+    in8 = (o & 2u) ? t : in8;
+    t = ((in8 & 0x0fu) << 4) | (in8 >> 4);
+    in8 = (o & 4u) ? t : in8;
+    return (hits & 0x00ffffffu) | (in8 << 24);
 }
 
 // Instance bounds (Params::inst_bounds, two words per InstRef, made by
@@ -552,7 +554,7 @@ __device__ __forceinline__ int trav_step(Trav& s, const Params& P, uint2* stack,
             if (s.ng.y > 0x00ffffffu) trav_push(P, stack, s.sp, s.ng);
         }
         uint32_t cb, pb, im;
-        const uint32_t hm = intersect_node<PACKED>(P.nodes, s.next, s.cur, s.tmax, cb, pb, im);
+        const uint32_t hm = intersect_node<PACKED>(P.nodes, P.node_words, s.next, s.cur, s.tmax, cb, pb, im);
         s.next = -1;
         s.ng = make_uint2(cb, (hm & 0xff000000u) | im);
         s.pbase = pb;
