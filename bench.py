@@ -149,13 +149,13 @@ class ClockSampler:
 # of one ncu-captured 1-spp frame (the autotuned launch configuration) / the
 # frame's 3.42 M closest-hit queries.  Traffic grows with the rays of a
 # launch: path-state reads and writes, BVH misses in L2.
-EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 90.4}
+EXTEND_DRAM_BYTES_PER_RAY = {"icosphere_1m": 93.8}
 # Warp-level instructions executed per closest-hit query by wf_extend on the
 # same capture (smsp__inst_executed.sum of the nine launches / the frame's
-# queries; camera rays take 177, the first bounce's rays 300): the
+# queries; camera rays take 166, the first bounce's rays about 290): the
 # numerator of the instruction-issue roofline (4 warp instructions per cycle
 # per SM).
-EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 223.4}
+EXTEND_WARP_INST_PER_RAY = {"icosphere_1m": 214.3}
 
 
 def bytes_per_ray(scene, options, camera, row_step=64, passes=2):
