@@ -575,6 +575,8 @@ def main():
     rays = 0
     launches = 0
     truncated = 0
+    untraced = 0
+    shadow_q = 0
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -587,6 +589,8 @@ def main():
             rays += st["closest"] + st["shadow"]
             launches += st["launches"]
             truncated += st["truncated"]
+            untraced += st["untraced"]
+            shadow_q += st["shadow"]
             if st["status"] != 0:
                 raise RuntimeError(f"kernel status {st['status']}")
         torch.cuda.synchronize()
@@ -594,6 +598,7 @@ def main():
         dist.barrier()
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_total = sum(ms) / 1000.0
+    rays_local = rays
     if dist:
         t = torch.tensor([t_total, float(rays)], dtype=torch.float64, device="cuda")
         tmax = t.clone()
@@ -602,6 +607,11 @@ def main():
         t_total, rays = float(tmax[0]), int(t[1])
     value = rays / t_total / 1e6
     rays_per_step = rays / (args.steps * world)
+    # the queries each kind of traversal ran (this rank's shares): shadow
+    # queries answered without traversal move none of their algorithmic bytes
+    loc = max(rays_local, 1)
+    closest_ps = rays_per_step * (rays_local - shadow_q) / loc
+    shadow_traced_ps = rays_per_step * (shadow_q - untraced) / loc
 
     # the other integrator on the same frame, same timing rules (the two give
     # the same accumulation up to last-bit rounding, so equal RMSE)
@@ -644,7 +654,7 @@ def main():
                 r.render_passes(base3 + k * spp, spp)
             st = r.stats()
             st_rays["closest"] += st["closest"]
-            st_rays["shadow"] += st["shadow"]
+            st_rays["shadow"] += st["shadow"] - st["untraced"]  # traversed by wf_shadow
             for name, (ms_k, n_k) in r.stage_stats().items():
                 tot[name][0] += ms_k
                 tot[name][1] += n_k
@@ -698,7 +708,8 @@ def main():
         peak, peak_kind = measured_peaks()
         b_ray, work = bytes_per_ray(sd, sd.render_options(), cam)
         mean_ms = statistics.mean(ms)
-        achieved = b_ray * rays_per_step / (mean_ms / 1000.0) / 1e9
+        achieved = (work["bytes_per_closest_ray"] * closest_ps + work["bytes_per_shadow_ray"] * shadow_traced_ps) \
+            / (mean_ms / 1000.0) / 1e9
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                     "kernel": "whole frame", "bytes_per_ray": b_ray, **work}
@@ -723,7 +734,7 @@ def main():
             # per query, against the nominal FP32 rate) and instruction
             # issue of the dominant kernel (ncu's instructions per query)
             fpk, nsm, mhz = fp32_peak_tflops()
-            f_ach = work["flops_per_ray"] * rays_per_step / (mean_ms / 1000.0) / 1e12
+            f_ach = work["flops_per_ray"] * (closest_ps + shadow_traced_ps) / (mean_ms / 1000.0) / 1e12
             fp32 = {"achieved": f_ach, "peak": fpk, "unit": "TFLOP/s", "frac": f_ach / fpk,
                     "flops_per_ray": work["flops_per_ray"],
                     "peak_source": f"nominal: {nsm} SMs x 128 FP32 lanes x 2 x {mhz:.0f} MHz"}
@@ -755,7 +766,11 @@ def main():
                        "parallelism": f"{world} rank(s), disjoint sample-pass ranges" if world > 1 else "1 GPU",
                        "tuning": tuning if tuning else "default",
                        "bvh": f"built on the GPU in {r.gpu_build_ms():.1f} ms" if args.gpu_bvh else "host collapse",
-                       "truncated_paths_per_step": truncated / args.steps},
+                       "truncated_paths_per_step": truncated / args.steps,
+                       # shadow queries of rays_per_step whose contribution is never added
+                       # (zero scattering pdf towards the light): answered without traversal
+                       "untraced_shadow_rays_per_step": untraced / args.steps,
+                       "traversed_rays_per_step": closest_ps + shadow_traced_ps},
             "gpu_launches": launches,
             "roofline": roofline,
             "e2e": e2e,

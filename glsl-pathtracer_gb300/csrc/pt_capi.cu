@@ -393,7 +393,7 @@ int check_materials(const float* mats, int nm, int num_tex) {
 }
 
 int begin_launch(pt_context* c) {
-    CK(cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 5 * sizeof(unsigned long long), c->stream));
     CK(cudaMemsetAsync(c->status.p, 0, sizeof(int), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     return PT_OK;
@@ -616,7 +616,7 @@ int create(const pt_scene_desc* d, const pt_mesh_desc* meshes, const pt_render_o
         if ((rc = upload_envmap(c, d->envmap_rgb, d->envmap_cdf, d->envmap_width, d->envmap_height,
                                 d->envmap_total_sum)))
             break;
-        if ((e = c->counters.alloc(4)) != cudaSuccess || (e = c->status.alloc(1)) != cudaSuccess) {
+        if ((e = c->counters.alloc(5)) != cudaSuccess || (e = c->status.alloc(1)) != cudaSuccess) {
             rc = cuda_err(e, "counters");
             break;
         }
@@ -828,7 +828,7 @@ int pt_batch_create(pt_context* const* jobs, int32_t n, pt_batch** out) {
         if (e == cudaSuccess) e = make_inst_bounds(b->inst_bounds, b->nodes.p, b->insts.p, ref_off, b->stream);
         if (e == cudaSuccess) e = make_node_words(b->node_words, b->nodes.p, node_off, b->stream);
         if (e != cudaSuccess) { rc = cuda_err(e, "batch index fix-up"); break; }
-        if ((e = b->counters.alloc(4)) != cudaSuccess || (e = b->status.alloc(1)) != cudaSuccess ||
+        if ((e = b->counters.alloc(5)) != cudaSuccess || (e = b->status.alloc(1)) != cudaSuccess ||
             (e = b->remaining.alloc(n)) != cudaSuccess || (e = b->done.alloc(n + 1)) != cudaSuccess) {
             rc = cuda_err(e, "batch buffers");
             break;
@@ -962,7 +962,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     CK(b->job_table.upload(entries.data(), entries.size(), b->stream));
     CK(cudaMemcpyAsync(b->remaining.p, remaining.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
     CK(cudaMemsetAsync(b->done.p, 0, sizeof(unsigned long long) * (n + 1), b->stream));
-    CK(cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(unsigned long long), b->stream));
+    CK(cudaMemsetAsync(b->counters.p, 0, 5 * sizeof(unsigned long long), b->stream));
     CK(cudaMemsetAsync(b->status.p, 0, sizeof(int), b->stream));
     Params p{};
     p.nodes = reinterpret_cast<const uint4*>(b->nodes.p);
@@ -1037,7 +1037,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
         CK(cudaEventRecord(b->ev1, b->stream));
     }
     std::vector<unsigned long long> done(n + 1);
-    unsigned long long cnt[4];
+    unsigned long long cnt[5];
     int st = 0;
     CK(cudaMemcpyAsync(done.data(), b->done.p, sizeof(unsigned long long) * (n + 1), cudaMemcpyDeviceToHost,
                        b->stream));
@@ -1050,6 +1050,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     b->last.shadow_rays = cnt[1];
     b->last.paths = cnt[2];
     b->last.truncated_paths = cnt[3];
+    b->last.untraced_shadow_rays = cnt[4];
     b->last.kernel_ms = ms;
     b->last.status = st;
     b->last.kernel_launches = launches;
@@ -1752,7 +1753,7 @@ int pt_get_stage_stats(pt_context* c, pt_stage_stats* s) {
 
 int pt_get_stats(pt_context* c, pt_stats* s) {
     if (!c || !s) return set_err(PT_ERR_INVALID_ARG, "NULL argument");
-    unsigned long long cnt[4] = {0, 0, 0, 0};
+    unsigned long long cnt[5] = {0, 0, 0, 0, 0};
     int st = 0;
     CK(cudaMemcpyAsync(cnt, c->counters.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&st, c->status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1763,6 +1764,7 @@ int pt_get_stats(pt_context* c, pt_stats* s) {
     s->shadow_rays = cnt[1];
     s->paths = cnt[2];
     s->truncated_paths = cnt[3];
+    s->untraced_shadow_rays = cnt[4];
     s->kernel_ms = ms;
     s->status = st;
     s->kernel_launches = c->launches;

@@ -832,4 +832,13 @@ __device__ __forceinline__ void add_counters(const Params& P, uint32_t closest, 
     }
 }
 
+// Shadow queries answered without traversal because their contribution is
+// never added (wf_shade, wf_shadow); they are counted among the shadow
+// queries as well.
+__device__ __forceinline__ void add_untraced(const Params& P, uint32_t n) {
+    const unsigned mask = __activemask();
+    n = __reduce_add_sync(mask, n);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1 && n) atomicAdd(P.counters + 4, (unsigned long long)n);
+}
+
 }  // namespace ptgb

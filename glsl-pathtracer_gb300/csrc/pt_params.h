@@ -96,7 +96,9 @@ struct Params {
     int width, height, tile_w, tile_h, ntx, nty;
     // output / bookkeeping
     float4* accum;
-    unsigned long long* counters;  // [0] closest-hit queries, [1] shadow queries, [2] paths
+    // [0] closest-hit queries, [1] shadow queries, [2] paths, [3] paths ended
+    // at PT_MAX_PATH_ITERATIONS, [4] shadow queries answered without traversal
+    unsigned long long* counters;
     int* status;                   // PT_OK or a PT_ERR_* code set by the kernels
     // traversal stack entries a ray may push (kStackSize; a lower bound is a
     // failure-detection test's way to make the overflow status fire)

@@ -583,6 +583,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
     const int* queue = resume ? B.qr : B.q[in];
     const int n = resume ? B.counts[6] : B.counts[in];
     Counters cnt{0, 0};
+    uint32_t untraced = 0;
     for (int j0 = blockIdx.x * blockDim.x; j0 < n; j0 += gridDim.x * blockDim.x) {
         const int j = j0 + threadIdx.x;
         const bool valid = j < n;
@@ -663,6 +664,18 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
             if (REPLAY && sr.suspended) {
                 shadow = true;  // to the transmittance queue; the path state stays as it was
             } else {
+                // Shadow queries whose contribution is never added (sr.adds
+                // clear: the scattering pdf towards the light is 0, as for a
+                // light below an opaque surface) need no traversal: their
+                // answer changes nothing, and the shadow stage draws no
+                // random numbers.  They count as queries, as the megakernel
+                // and the reference trace them (pathtrace.glsl:198-209 and
+                // 264-275 trace first and evaluate the BSDF after).
+                if (!INLINE && MEDIUM != 2 && sr.n != 0 && sr.adds == 0) {
+                    cnt.shadow += __popc(sr.n);
+                    untraced += __popc(sr.n);
+                    sr.n = 0;
+                }
                 shadow = !INLINE && sr.n != 0;
                 // a path that ends here with no shadow query pending needs
                 // only its radiance (B.rad, below)
@@ -706,6 +719,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
         push(B.qs, B.counts + 2, i, valid && shadow);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
+    add_untraced(P, untraced);
     if (ADJ) adj_flush(A, sgrad);
 }
 
@@ -722,6 +736,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
     const int n = B.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) B.counts[4] = 0;  // fetch counter of the next extend stage
     Counters cnt{0, 0};
+    uint32_t untraced = 0;
     Trav s;
     // per-thread stage: 0 start env ray, 1 tracing it, 2 start light ray,
     // 3 tracing it, 4 both resolved
@@ -733,7 +748,13 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
     auto start = [&]() {
         if (path >= 0 && (stage == 0 || stage == 2)) {
             const int which = stage >> 1;
-            if (bits & (1 << which)) {
+            if ((bits & (1 << which)) && !(bits & (4 << which))) {
+                // a query whose contribution is never added (the other one
+                // of this path is): counted, not traced (wf_shade)
+                cnt.shadow++;
+                untraced++;
+                stage += 2;
+            } else if (bits & (1 << which)) {
                 const float4 d = which ? B.sd1[path] : B.sd0[path];
                 const Ray r{origin, v3(d.x, d.y, d.z)};
                 cnt.shadow++;
@@ -843,6 +864,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
         }
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
+    add_untraced(P, untraced);
     if (ADJ) adj_flush(A, sgrad);
 }
 

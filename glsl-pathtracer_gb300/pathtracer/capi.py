@@ -79,7 +79,7 @@ class pt_stats(C.Structure):
     _fields_ = [
         ("closest_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
         ("kernel_ms", C.c_float), ("status", C.c_int32), ("kernel_launches", C.c_int32),
-        ("truncated_paths", C.c_uint64),
+        ("truncated_paths", C.c_uint64), ("untraced_shadow_rays", C.c_uint64),
     ]
 
 

@@ -123,7 +123,8 @@ class GpuRenderer:
         s = capi.pt_stats()
         self._ck(self.lib.pt_get_stats(self.ctx, C.byref(s)))
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
-                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths)
+                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths,
+                    untraced=s.untraced_shadow_rays)
 
     def update_materials(self, materials: np.ndarray):
         m = np.ascontiguousarray(materials, np.float32)
@@ -226,7 +227,8 @@ class GpuBatch:
         s = capi.pt_stats()
         capi.check(self.lib, self.lib.pt_batch_stats(self.handle, C.byref(s)))
         return dict(closest=s.closest_rays, shadow=s.shadow_rays, paths=s.paths, kernel_ms=s.kernel_ms,
-                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths)
+                    status=s.status, launches=s.kernel_launches, truncated=s.truncated_paths,
+                    untraced=s.untraced_shadow_rays)
 
     def close(self):
         if self.handle:

@@ -147,12 +147,17 @@ typedef struct pt_hit {
 /* Counters of the last render call. */
 typedef struct pt_stats {
     uint64_t closest_rays;           /* executed closest-hit queries */
-    uint64_t shadow_rays;            /* executed any-hit queries / transmittance segments */
+    uint64_t shadow_rays;            /* any-hit queries / transmittance segments the
+                                        reference traces, untraced_shadow_rays included */
     uint64_t paths;                  /* camera paths traced */
     float    kernel_ms;              /* device time of the last render call (CUDA events) */
     int32_t  status;                 /* device status word of the last call (PT_OK or PT_ERR_*) */
     int32_t  kernel_launches;        /* kernels the last render call launched */
     uint64_t truncated_paths;        /* paths ended at PT_MAX_PATH_ITERATIONS */
+    uint64_t untraced_shadow_rays;   /* of shadow_rays: answered without traversal by the
+                                        wavefront, because their contribution is never added
+                                        (the scattering pdf towards the light is 0); the
+                                        reference traces them and then discards the result */
 } pt_stats;
 
 #define PT_INTEGRATOR_MEGAKERNEL 0

@@ -271,6 +271,33 @@ def test_wavefront_equals_megakernel(ptlib, name):
     assert rel.max() < 1e-4 and np.mean(rel) < 1e-6, (rel.max(), np.mean(rel))
 
 
+def test_untraced_shadow_queries(ptlib):
+    """The wavefront answers shadow queries whose contribution is never added
+    (the scattering pdf towards the light is 0: lights below an opaque
+    surface) without traversal; they still count as shadow queries, so the
+    totals equal the megakernel's, which traces every one, and the
+    accumulation is the megakernel's."""
+    from pathtracer import capi
+    from pathtracer.renderer import GpuRenderer
+    sd = scene_by_name("icosphere")
+    with GpuRenderer(sd) as r:
+        r.render_passes(0, 2)
+        a = r.accum()
+        sa = r.stats()
+        r.clear()
+        r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        r.render_passes(0, 2)
+        b = r.accum()
+        sb = r.stats()
+    assert sa["status"] == 0 and sb["status"] == 0
+    assert sa["untraced"] == 0
+    assert 0 < sb["untraced"] < sb["shadow"], sb
+    assert sa["closest"] + sa["shadow"] == sb["closest"] + sb["shadow"]
+    assert np.array_equal(a[..., 3], b[..., 3])
+    rel = np.abs(a[..., :3] - b[..., :3]) / np.maximum(np.abs(b[..., :3]), 1e-3)
+    assert rel.max() < 1e-4 and np.mean(rel) < 1e-6, (rel.max(), np.mean(rel))
+
+
 def test_wavefront_batches_and_tiles(ptlib, monkeypatch):
     """Small wavefront batches (several batches per call, one pass each) and
     single tiles give the megakernel's accumulation."""
