@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include <cmath>
 #include <cstdlib>
 
 #include "../../include/pt_cuda.h"
@@ -82,6 +83,13 @@ struct pt_context {
     WideBVH bvh{};
     std::vector<float> bin_nodes;  // host copy of the binary BVH (TLAS updates)
     int top_level_index = 0;
+    // VOL_MIS transmittance queries whose contribution is never added may go
+    // untraced (Params::untraced bit 1): world boxes of the blended-alpha
+    // instances (update_blend_boxes)
+    std::vector<float> host_mats;
+    DevBuf<float> blend_boxes;
+    int num_blend_boxes = 0;
+    bool untraced_transmit = false;
     int num_tris = 0, num_vertices = 0, num_materials = 0, num_instances = 0, num_lights = 0;
     int env_w = 0, env_h = 0;
     float env_total = 0.0f;
@@ -220,6 +228,14 @@ uint32_t option_flags(const pt_context* c) {
     return f;
 }
 
+// Params::untraced for a render: PT_UNTRACED_SHADOWS=0 traces every shadow
+// query (the same images; for comparisons).
+int untraced_bits(bool transmit) {
+    const char* e = std::getenv("PT_UNTRACED_SHADOWS");
+    if (e && std::atoi(e) == 0) return 0;
+    return 1 | (transmit ? 2 : 0);
+}
+
 Params make_params(const pt_context* c) {
     Params p{};
     p.nodes = reinterpret_cast<const uint4*>(c->nodes.p);
@@ -277,6 +293,9 @@ Params make_params(const pt_context* c) {
     p.counters = c->counters.p;
     p.status = c->status.p;
     p.stack_limit = c->stack_limit;
+    p.untraced = untraced_bits(c->untraced_transmit);
+    p.blend_boxes = c->blend_boxes.p;
+    p.num_blend_boxes = c->num_blend_boxes;
     return p;
 }
 
@@ -378,6 +397,46 @@ uint32_t scene_flags_of(const float* mats, int nm, int nl) {
         if ((int)mats[32 * i + 18] != MEDIUM_NONE) f |= F_MEDIUM;            // Renderer.cpp:455-461
     }
     return f;
+}
+
+// Where VOL_MIS transmittance queries whose contribution is never added may
+// go untraced (DirectLight): EvalTransmittance draws random numbers only at
+// blended-alpha hits (pathtrace.glsl:133), so a query whose ray meets none
+// of the blended instances' world boxes draws none; and it ends at its first
+// hit (one segment) when no other instance's material is refractive or
+// alpha-masked (pathtrace.glsl:134-138).  The boxes are the TLAS leaves of
+// the reference's binary BVH, widened by 1e-4 of their largest coordinate
+// plus 1e-4.  Not for BVHs built on the GPU (no binary TLAS), and not beyond
+// kMaxBlendBoxes blended instances.
+constexpr int kMaxBlendBoxes = 16;
+int update_blend_boxes(pt_context* c) {
+    c->untraced_transmit = false;
+    c->num_blend_boxes = 0;
+    if (c->gpu_bvh || c->bin_nodes.empty() || c->host_mats.empty()) return PT_OK;
+    const float* mats = c->host_mats.data();
+    const size_t total = c->bin_nodes.size() / 9;
+    std::vector<float> boxes;
+    for (size_t i = (size_t)c->top_level_index; i < total; ++i) {
+        const float* p = c->bin_nodes.data() + 9 * i;
+        if (!(p[8] < 0.0f)) continue;  // TLAS leaf: LRLeaf.z = -instance - 1, material in LRLeaf.y
+        const float* m = mats + 32 * (size_t)(int)p[7];
+        const int alpha = (int)m[29];
+        if (alpha == ALPHA_MODE_BLEND) {
+            if (boxes.size() >= 6 * (size_t)kMaxBlendBoxes) return PT_OK;
+            double ext = 0.0;
+            for (int k = 0; k < 6; ++k) ext = std::max(ext, std::fabs((double)p[k]));
+            const float w = (float)(1e-4 * (1.0 + ext));
+            for (int k = 0; k < 3; ++k) boxes.push_back(p[k] - w);
+            for (int k = 3; k < 6; ++k) boxes.push_back(p[k] + w);
+        } else if (alpha == ALPHA_MODE_MASK || m[16] > 0.0f) {  // masked, or specTrans > 0
+            return PT_OK;
+        }
+    }
+    CK(c->blend_boxes.upload(boxes.data(), boxes.size(), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->num_blend_boxes = (int)(boxes.size() / 6);
+    c->untraced_transmit = true;
+    return PT_OK;
 }
 
 // Texture ids of a material (Material.h:87-119, texIDs at 24..27) index the
@@ -592,7 +651,9 @@ int create(const pt_scene_desc* d, const pt_mesh_desc* meshes, const pt_render_o
         c->num_instances = d->num_instances;
         c->num_lights = d->num_lights;
         c->scene_flags = scene_flags_of(d->materials, d->num_materials, d->num_lights);
+        c->host_mats.assign(d->materials, d->materials + 32 * (size_t)d->num_materials);
         if (!meshes && (rc = upload_bvh(c))) break;
+        if ((rc = update_blend_boxes(c))) break;
         if ((rc = upload_instances(c, d->transforms, d->num_instances))) break;
         if ((e = c->vidx.upload(d->vert_indices, 3 * (size_t)d->num_tris, c->stream)) != cudaSuccess ||
             (e = c->verts.upload(d->vertices_uvx, d->num_vertices, c->stream)) != cudaSuccess ||
@@ -982,6 +1043,7 @@ int pt_batch_render(pt_batch* b, const int32_t* first_pass, const int32_t* num_p
     p.status = b->status.p;
     p.stack_limit = kStackSize;
     for (pt_context* c : b->jobs) p.stack_limit = std::min(p.stack_limit, c->stack_limit);
+    p.untraced = untraced_bits(false);  // batches hold no VOL_MIS media
     p.jobs = b->job_table.p;
     p.num_jobs = (int)entries.size();
     // every job enters its BLAS directly: the direct form of the traversal
@@ -1095,7 +1157,7 @@ int pt_destroy(pt_context* c) {
     c->nodes.free(); c->tris.free(); c->insts.free(); c->xf.free(); c->inst_bounds.free(); c->node_words.free(); c->vidx.free(); c->verts.free();
     c->norms.free(); c->mats.free(); c->lights.free(); c->env.free(); c->cdf.free(); c->accum.free();
     c->tex.free();
-    c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free();
+    c->snapshot.free(); c->ldr.free(); c->counters.free(); c->status.free(); c->blend_boxes.free();
     wavefront_free(c->wf);
     c->timer.release();
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1165,9 +1227,10 @@ int pt_update_instances(pt_context* c, const float* transforms, int32_t num_inst
         CK(c->mats.upload(materials, 8 * (size_t)num_materials, c->stream));
         c->num_materials = num_materials;
         c->scene_flags = scene_flags_of(materials, num_materials, c->num_lights);
+        c->host_mats.assign(materials, materials + 32 * (size_t)num_materials);
     }
     CK(cudaStreamSynchronize(c->stream));
-    return PT_OK;
+    return update_blend_boxes(c);
 }
 
 int pt_update_envmap(pt_context* c, const float* rgb, const float* cdf, int32_t w, int32_t h, float total) {
@@ -1267,8 +1330,9 @@ int pt_update_materials(pt_context* c, const float* materials, int32_t num_mater
     CK(c->mats.upload(materials, 8 * (size_t)num_materials, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->scene_flags = scene_flags_of(materials, num_materials, c->num_lights);
+    c->host_mats.assign(materials, materials + 32 * (size_t)num_materials);
     c->version++;
-    return PT_OK;
+    return update_blend_boxes(c);
 }
 
 int pt_update_lights(pt_context* c, const float* lights, int32_t num_lights) {

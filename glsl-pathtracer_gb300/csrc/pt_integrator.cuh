@@ -62,6 +62,7 @@ struct ShadowReq {
 
 struct Counters {
     uint32_t closest, shadow;
+    uint32_t untraced;  // of shadow: answered without traversal (DirectLight)
 };
 
 // ------------------------------------------------------------ ClosestHit
@@ -448,9 +449,40 @@ __device__ __forceinline__ V3 ScatterEval(bool isSurface, const Material& mat, f
     return v3(p);
 }
 
+// Whether the ray (t >= 0) may meet one of the world boxes of the scene's
+// blended-alpha instances (Params::blend_boxes): the only geometry at which
+// EvalTransmittance draws random numbers.  Slab test in FP32 against boxes
+// the host has widened; a NaN in the test counts as a meeting.
+__device__ __forceinline__ bool may_cross_blend(const Params& P, const Ray& r) {
+    for (int k = 0; k < P.num_blend_boxes; ++k) {
+        const float* b = P.blend_boxes + 6 * k;
+        float t0 = 0.0f, t1 = PT_INF;
+        bool miss = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float o = a == 0 ? r.origin.x : a == 1 ? r.origin.y : r.origin.z;
+            const float d = a == 0 ? r.direction.x : a == 1 ? r.direction.y : r.direction.z;
+            if (d == 0.0f) {
+                if (o < b[a] || o > b[3 + a]) miss = true;
+                continue;
+            }
+            const float ta = (b[a] - o) / d, tb = (b[3 + a] - o) / d;
+            t0 = fmaxf(t0, fminf(ta, tb));
+            t1 = fminf(t1, fmaxf(ta, tb));
+        }
+        if (!miss && !(t0 > t1)) return true;
+    }
+    return false;
+}
+
 // pathtrace.glsl:158-283.  INLINE: shadow rays traced here and the result
 // returned; otherwise the rays and their contributions go to `sr` and the
 // caller adds the unoccluded ones (same values, same order).
+// A VOL_MIS query whose contribution is never added (the scattering pdf
+// towards the light is 0) is answered without traversal when Params::
+// untraced allows it and its ray cannot meet blended geometry: its result
+// is discarded, and it draws no random numbers and runs one segment in the
+// reference (pathtrace.glsl:117-153), which the counters record.
 template <int MEDIUM, bool ENV, bool INLINE, class Hook>
 __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp, V3 normal, V3 ffnormal,
                                           const Material& mat, float eta, const Medium& medium, bool isSurface,
@@ -472,17 +504,25 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
         }
         const Ray shadowRay{scatterPos, lightDir};
         if (volmis && INLINE) {
-            V3 Tr;
-            if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
-                sr.suspended = true;
-                return Ld;
-            }
-            Li = Li * Tr;
             float sfPdf;
             const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, lightDir, sfPdf);
-            if (sfPdf > 0.0f) {
-                float misWeight = PowerHeuristic(lightPdf, sfPdf);
-                if (misWeight > 0.0f) Ld = Ld + misWeight * Li * sf * P.env_intensity / lightPdf;
+            const bool adds = sfPdf > 0.0f && PowerHeuristic(lightPdf, sfPdf) > 0.0f;
+            if (!adds && (P.untraced & 2) && !may_cross_blend(P, shadowRay)) {
+                if (hook.first_visit()) {
+                    cnt.shadow++;
+                    cnt.untraced++;
+                }
+            } else {
+                V3 Tr;
+                if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
+                    sr.suspended = true;
+                    return Ld;
+                }
+                Li = Li * Tr;
+                if (sfPdf > 0.0f) {
+                    float misWeight = PowerHeuristic(lightPdf, sfPdf);
+                    if (misWeight > 0.0f) Ld = Ld + misWeight * Li * sf * P.env_intensity / lightPdf;
+                }
             }
         } else if (volmis) {  // transmittance deferred to the transmittance stage
             float sfPdf;
@@ -541,17 +581,24 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
         if (dot(ls.direction, ls.normal) < 0.0f) {
             const Ray shadowRay{scatterPos, ls.direction};
             if (volmis && INLINE) {
-                V3 Tr;
-                if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
-                    sr.suspended = true;
-                    return Ld;
-                }
-                Li = Li * Tr;
                 float sfPdf;
                 const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, ls.direction, sfPdf);
-                float misWeight = 1.0f;
-                if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
-                if (sfPdf > 0.0f) Ld = Ld + misWeight * sf * Li / ls.pdf;
+                if (!(sfPdf > 0.0f) && (P.untraced & 2) && !may_cross_blend(P, shadowRay)) {
+                    if (hook.first_visit()) {
+                        cnt.shadow++;
+                        cnt.untraced++;
+                    }
+                } else {
+                    V3 Tr;
+                    if (!hook.transmit(P, shadowRay, rng, stack, cnt, Tr)) {
+                        sr.suspended = true;
+                        return Ld;
+                    }
+                    Li = Li * Tr;
+                    float misWeight = 1.0f;
+                    if (light.area > 0.0f) misWeight = PowerHeuristic(ls.pdf, sfPdf);
+                    if (sfPdf > 0.0f) Ld = Ld + misWeight * sf * Li / ls.pdf;
+                }
             } else if (volmis) {  // transmittance deferred to the transmittance stage
                 float sfPdf;
                 const V3 sf = ScatterEval(isSurface, mat, eta, V, ffnormal, medium.anisotropy, ls.direction, sfPdf);
@@ -632,6 +679,9 @@ struct NoHook {
     // the RNG state it left); env_sampled sees a sample just drawn
     __device__ __forceinline__ bool env_sample(V3&, float&, V3&) { return false; }
     __device__ __forceinline__ void env_sampled(V3, float, V3) {}
+    // whether this run of the step reaches the point for the first time (a
+    // re-run of a suspended step repeats the part before its last query)
+    __device__ __forceinline__ bool first_visit() const { return true; }
 };
 
 // One iteration of PathTrace's loop (pathtrace.glsl:301-473) for the hit in

@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(128) render_kernel(Params P, RenderWork W) {
         *out = acc;
     }
     add_counters(P, cnt.closest, cnt.shadow, paths);
+    add_untraced(P, cnt.untraced);
 }
 
 __global__ void __launch_bounds__(128) trace_closest_kernel(Params P, const pt_ray* __restrict__ rays, int n,

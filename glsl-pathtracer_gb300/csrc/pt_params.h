@@ -103,6 +103,14 @@ struct Params {
     // traversal stack entries a ray may push (kStackSize; a lower bound is a
     // failure-detection test's way to make the overflow status fire)
     int stack_limit;
+    // shadow queries whose contribution is never added are answered without
+    // traversal: bit 0 any-hit queries (always), bit 1 VOL_MIS transmittance
+    // queries (when a query cannot draw random numbers or take more than one
+    // segment unless its ray meets one of the num_blend_boxes world boxes of
+    // blended-alpha instances, 6 floats each: lo, hi); 0 turns both off
+    int untraced;
+    const float* blend_boxes;
+    int num_blend_boxes;
     // batches (pt_batch_render): the jobs, paths left per job and the
     // %globaltimer at which each job's last path finished ([num_jobs]: start)
     const BatchJob* jobs;

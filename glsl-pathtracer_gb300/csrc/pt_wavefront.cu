@@ -86,6 +86,8 @@ struct ReplayHook : NoHook {
         env_dir = dir;
         env_new = true;
     }
+    // queries before `done` were reached by an earlier run of this step
+    __device__ __forceinline__ bool first_visit() const { return site >= done; }
     __device__ __forceinline__ bool transmit(const Params&, const Ray& r, Rng& rng, uint2*, Counters&, V3& T) {
         if (site < done) {
             const float4 t = site ? B->tr1[i] : B->tr0[i];
@@ -554,6 +556,7 @@ struct AdjHook {
     }
     __device__ __forceinline__ bool env_sample(V3&, float&, V3&) { return false; }
     __device__ __forceinline__ void env_sampled(V3, float, V3) {}
+    __device__ __forceinline__ bool first_visit() const { return true; }
 };
 
 __device__ __forceinline__ float* adj_accumulator(const AdjView& A, float* sgrad) {
@@ -671,10 +674,19 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
                 // random numbers.  They count as queries, as the megakernel
                 // and the reference trace them (pathtrace.glsl:198-209 and
                 // 264-275 trace first and evaluate the BSDF after).
-                if (!INLINE && MEDIUM != 2 && sr.n != 0 && sr.adds == 0) {
+                if (!INLINE && MEDIUM != 2 && (P.untraced & 1) && sr.n != 0 && sr.adds == 0) {
                     cnt.shadow += __popc(sr.n);
                     untraced += __popc(sr.n);
                     sr.n = 0;
+                }
+                // the same for deferred transmittance queries (no alpha
+                // materials in this form, so none draws random numbers; one
+                // segment each when Params::untraced allows it)
+                if (!INLINE && !REPLAY && MEDIUM == 2 && (P.untraced & 2) && (sr.n & ~sr.adds & 3)) {
+                    const int drop = sr.n & ~sr.adds & 3;
+                    cnt.shadow += __popc(drop);
+                    untraced += __popc(drop);
+                    sr.n &= ~drop;
                 }
                 shadow = !INLINE && sr.n != 0;
                 // a path that ends here with no shadow query pending needs
@@ -719,7 +731,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shade(Params P, WfView B, int in
         push(B.qs, B.counts + 2, i, valid && shadow);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
-    add_untraced(P, untraced);
+    add_untraced(P, untraced + cnt.untraced);
     if (ADJ) adj_flush(A, sgrad);
 }
 
@@ -748,7 +760,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
     auto start = [&]() {
         if (path >= 0 && (stage == 0 || stage == 2)) {
             const int which = stage >> 1;
-            if ((bits & (1 << which)) && !(bits & (4 << which))) {
+            if ((bits & (1 << which)) && !(bits & (4 << which)) && (P.untraced & 1)) {
                 // a query whose contribution is never added (the other one
                 // of this path is): counted, not traced (wf_shade)
                 cnt.shadow++;
@@ -864,7 +876,7 @@ __global__ void __launch_bounds__(128, MINB) wf_shadow(Params P, WfView B, int r
         }
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
-    add_untraced(P, untraced);
+    add_untraced(P, untraced + cnt.untraced);
     if (ADJ) adj_flush(A, sgrad);
 }
 
@@ -1041,6 +1053,7 @@ __global__ void __launch_bounds__(128) wf_tail(Params P, WfView B, int in, int r
         if (BATCH) job_path_done(P, ps.job);
     }
     add_counters(P, cnt.closest, cnt.shadow, 0);
+    add_untraced(P, cnt.untraced);
 }
 
 // TransmitStep out of line with the path's RNG (replay: blended materials

@@ -298,6 +298,37 @@ def test_untraced_shadow_queries(ptlib):
     assert rel.max() < 1e-4 and np.mean(rel) < 1e-6, (rel.max(), np.mean(rel))
 
 
+@pytest.mark.parametrize("name,integrator", [
+    ("icosphere", "wavefront"), ("instanced", "wavefront"), ("instanced", "megakernel"),
+    ("ref_volume", "wavefront"), ("ref_volume", "megakernel"),
+])
+def test_untraced_queries_change_nothing(ptlib, monkeypatch, name, integrator):
+    """Shadow and transmittance queries answered without traversal change no
+    result: the accumulation is bit for bit the one with every query traced
+    (PT_UNTRACED_SHADOWS=0), and the query counts are the same."""
+    from pathtracer import capi
+    from pathtracer.renderer import GpuRenderer
+    sd = scene_by_name(name)
+    with GpuRenderer(sd) as r:
+        if integrator == "wavefront":
+            r.set_integrator(capi.PT_INTEGRATOR_WAVEFRONT)
+        monkeypatch.setenv("PT_UNTRACED_SHADOWS", "0")
+        r.render_passes(0, 2)
+        a = r.accum()
+        sa = r.stats()
+        r.clear()
+        monkeypatch.delenv("PT_UNTRACED_SHADOWS")
+        r.render_passes(0, 2)
+        b = r.accum()
+        sb = r.stats()
+    assert sa["status"] == 0 and sb["status"] == 0
+    assert sa["untraced"] == 0
+    if name != "ref_volume":  # the icosphere's far side; VOL_MIS queries beside the blended volume
+        assert sb["untraced"] > 0, sb
+    assert np.array_equal(a, b)
+    assert sa["closest"] == sb["closest"] and sa["shadow"] == sb["shadow"], (sa, sb)
+
+
 def test_wavefront_batches_and_tiles(ptlib, monkeypatch):
     """Small wavefront batches (several batches per call, one pass each) and
     single tiles give the megakernel's accumulation."""
