@@ -154,10 +154,12 @@ typedef struct pt_stats {
     int32_t  status;                 /* device status word of the last call (PT_OK or PT_ERR_*) */
     int32_t  kernel_launches;        /* kernels the last render call launched */
     uint64_t truncated_paths;        /* paths ended at PT_MAX_PATH_ITERATIONS */
-    uint64_t untraced_shadow_rays;   /* of shadow_rays: answered without traversal by the
-                                        wavefront, because their contribution is never added
-                                        (the scattering pdf towards the light is 0); the
-                                        reference traces them and then discards the result */
+    uint64_t untraced_shadow_rays;   /* of shadow_rays: answered without traversal because
+                                        their contribution is never added (the scattering pdf
+                                        towards the light is 0): any-hit queries of the
+                                        wavefront, and VOL_MIS transmittance queries that
+                                        cannot meet blended geometry; the reference traces
+                                        them and then discards the result */
 } pt_stats;
 
 #define PT_INTEGRATOR_MEGAKERNEL 0
