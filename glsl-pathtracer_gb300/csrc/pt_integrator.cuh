@@ -883,8 +883,8 @@ __device__ __forceinline__ void add_counters(const Params& P, uint32_t closest, 
 }
 
 // Shadow queries answered without traversal because their contribution is
-// never added (wf_shade, wf_shadow); they are counted among the shadow
-// queries as well.
+// never added (DirectLight, wf_shade, wf_shadow); they are counted among the
+// shadow queries as well.
 __device__ __forceinline__ void add_untraced(const Params& P, uint32_t n) {
     const unsigned mask = __activemask();
     n = __reduce_add_sync(mask, n);
