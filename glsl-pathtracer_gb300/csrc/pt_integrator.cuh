@@ -264,12 +264,16 @@ __device__ __forceinline__ bool LightsAny(const Params& P, const Ray& r, float m
 }
 
 // anyhit.glsl:25-216
+// Whether AnyHit draws random numbers (the alpha test of anyhit.glsl:118-141,
+// which the reference compiles without media only).
+__device__ __forceinline__ bool any_hit_draws(const Params& P) {
+    return (P.flags & F_ALPHA_TEST) && !(P.flags & F_MEDIUM);
+}
 static __device__ __noinline__ bool AnyHit(const Params& P, const Ray& r, float maxDist, Rng& rng, uint2* stack,
                                            Counters& cnt) {
     cnt.shadow++;
     if (LightsAny(P, r, maxDist)) return true;
-    const bool alpha = (P.flags & F_ALPHA_TEST) && !(P.flags & F_MEDIUM);
-    return trace_any(P, r.origin, r.direction, maxDist, alpha, rng, stack);
+    return trace_any(P, r.origin, r.direction, maxDist, any_hit_draws(P), rng, stack);
 }
 
 // pathtrace.glsl:118-156 (OPT_MEDIUM && OPT_VOL_MIS); each segment is counted
@@ -478,11 +482,12 @@ __device__ __forceinline__ bool may_cross_blend(const Params& P, const Ray& r) {
 // pathtrace.glsl:158-283.  INLINE: shadow rays traced here and the result
 // returned; otherwise the rays and their contributions go to `sr` and the
 // caller adds the unoccluded ones (same values, same order).
-// A VOL_MIS query whose contribution is never added (the scattering pdf
-// towards the light is 0) is answered without traversal when Params::
-// untraced allows it and its ray cannot meet blended geometry: its result
-// is discarded, and it draws no random numbers and runs one segment in the
-// reference (pathtrace.glsl:117-153), which the counters record.
+// A query whose contribution is never added (the scattering pdf towards the
+// light is 0) is answered without traversal when Params::untraced allows it
+// and the query draws no random numbers: an any-hit query when AnyHit has no
+// alpha test, a VOL_MIS query when its ray cannot meet blended geometry
+// (then it runs one segment in the reference, pathtrace.glsl:117-153).  Its
+// result would be discarded; the counters record it as traced once.
 template <int MEDIUM, bool ENV, bool INLINE, class Hook>
 __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp, V3 normal, V3 ffnormal,
                                           const Material& mat, float eta, const Medium& medium, bool isSurface,
@@ -552,7 +557,17 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
                     }
                 }
             };
-            if (INLINE) {
+            if (INLINE && (P.untraced & 1) && !any_hit_draws(P)) {
+                // evaluated first: a query whose contribution is never
+                // added is answered without traversal
+                contribution();
+                if (!adds) {
+                    cnt.shadow++;
+                    cnt.untraced++;
+                } else if (!AnyHit(P, shadowRay, PT_INF - PT_EPS, rng, stack, cnt)) {
+                    Ld = Ld + c;
+                }
+            } else if (INLINE) {
                 if (!AnyHit(P, shadowRay, PT_INF - PT_EPS, rng, stack, cnt)) {
                     contribution();
                     if (adds) Ld = Ld + c;
@@ -625,7 +640,15 @@ __device__ __forceinline__ V3 DirectLight(const Params& P, const Ray& r, V3 fhp,
                         hook.nee_light(index, misWeight, Li, sf, ls.pdf, eta, V, ffnormal, ls.direction);
                     }
                 };
-                if (INLINE) {
+                if (INLINE && (P.untraced & 1) && !any_hit_draws(P)) {
+                    contribution();
+                    if (!adds) {
+                        cnt.shadow++;
+                        cnt.untraced++;
+                    } else if (!AnyHit(P, shadowRay, ls.dist - PT_EPS, rng, stack, cnt)) {
+                        Ld = Ld + c;
+                    }
+                } else if (INLINE) {
                     if (!AnyHit(P, shadowRay, ls.dist - PT_EPS, rng, stack, cnt)) {
                         contribution();
                         if (adds) Ld = Ld + c;

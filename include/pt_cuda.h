@@ -156,8 +156,8 @@ typedef struct pt_stats {
     uint64_t truncated_paths;        /* paths ended at PT_MAX_PATH_ITERATIONS */
     uint64_t untraced_shadow_rays;   /* of shadow_rays: answered without traversal because
                                         their contribution is never added (the scattering pdf
-                                        towards the light is 0): any-hit queries of the
-                                        wavefront, and VOL_MIS transmittance queries that
+                                        towards the light is 0): any-hit queries without an
+                                        alpha test, and VOL_MIS transmittance queries that
                                         cannot meet blended geometry; the reference traces
                                         them and then discards the result */
 } pt_stats;

@@ -272,11 +272,10 @@ def test_wavefront_equals_megakernel(ptlib, name):
 
 
 def test_untraced_shadow_queries(ptlib):
-    """The wavefront answers shadow queries whose contribution is never added
-    (the scattering pdf towards the light is 0: lights below an opaque
+    """Both integrators answer shadow queries whose contribution is never
+    added (the scattering pdf towards the light is 0: lights below an opaque
     surface) without traversal; they still count as shadow queries, so the
-    totals equal the megakernel's, which traces every one, and the
-    accumulation is the megakernel's."""
+    totals are equal, and the accumulation is the megakernel's."""
     from pathtracer import capi
     from pathtracer.renderer import GpuRenderer
     sd = scene_by_name("icosphere")
@@ -290,7 +289,7 @@ def test_untraced_shadow_queries(ptlib):
         b = r.accum()
         sb = r.stats()
     assert sa["status"] == 0 and sb["status"] == 0
-    assert sa["untraced"] == 0
+    assert 0 < sa["untraced"] < sa["shadow"], sa
     assert 0 < sb["untraced"] < sb["shadow"], sb
     assert sa["closest"] + sa["shadow"] == sb["closest"] + sb["shadow"]
     assert np.array_equal(a[..., 3], b[..., 3])
@@ -299,7 +298,7 @@ def test_untraced_shadow_queries(ptlib):
 
 
 @pytest.mark.parametrize("name,integrator", [
-    ("icosphere", "wavefront"), ("instanced", "wavefront"), ("instanced", "megakernel"),
+    ("icosphere", "wavefront"), ("icosphere", "megakernel"), ("instanced", "wavefront"), ("instanced", "megakernel"),
     ("ref_volume", "wavefront"), ("ref_volume", "megakernel"),
 ])
 def test_untraced_queries_change_nothing(ptlib, monkeypatch, name, integrator):
